@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Benchmark: pressure-Poisson solves per second to ||r||/||b|| <= 1e-10.
+
+Workload: the wavy-wall channel at 256x128x256 (8.4M cells, wall amplitude
+0.1, y-stretch 2.5, RHS seed 1), seeded synthetic inputs.  One step is one
+complete solve from a zero initial guess on the GPU-resident grid through
+the C ABI (ples_mg_solve_device): mixed precision, FP32 V-cycles inside the
+FP64 defect-correction loop.  `value` is whole-job solves/s (K steps x N
+replicas / max over ranks of the CUDA-event time on the solve stream).
+Inputs stay larger than L2 (the FP64 fields and coefficients are ~1.9 GB),
+so no L2 flush is needed between steps.
+
+Extra fields: the plain-FP64 solve rate on the same grid and the mixed/FP64
+ratio; `e2e` times the host-buffer entry point ples_mg_solve (pinned host
+fi/rhs, H2D and D2H inside the timed region); `roofline` measures the
+dominant kernel (the level-1 FP32 eta-line smoother) with CUDA events
+around each of its launches inside the timed region; `cpu_baseline` times
+the CPU oracle (the restated reference algorithm, line SOR, emulated MPI
+ranks as threads) on a bounded sample.
+
+`--impl reference` times the reference's algorithm on the host cores (the
+CPU oracle: the Fortran reference cannot be built here) and prints the same
+line with "impl": "reference".
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Poisson solves/s to rel-resid 1e-10"
+UNIT = "solves/s"
+# V-cycles the reference algorithm (line SOR, omega 1.6, 5/10 sweeps, 4
+# levels) needs to reach ||r||/||b|| <= 1e-10 on this workload, measured with
+# the CPU oracle (8 emulated ranks); the CPU baseline times a sample of
+# cycles and scales by this count.
+REF_CYCLES_TO_1E10 = {"channel_256x128x256": None}
+# algorithmic bytes per cell of one FP32 eta-line sweep: read p, rhs and the
+# nine face coefficients, write p (12 x 4 B)
+LINE_BYTES_PER_CELL = 48
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(workload, threads_cap=None, cycles=1):
+    """Reference algorithm on the host: the CPU oracle (line SOR as in the
+    reference's islor=1 option, 4 levels, kss 5/10, omega 1.6) with nproc
+    emulated MPI ranks as threads, timed over `cycles` V-cycles at the full
+    size and scaled to solves/s with the measured cycle count."""
+    from oracle.oracle import Oracle
+    from ples_gb300 import synthetic as S
+    w = S.WORKLOADS[workload]
+    x, y, z = w.grid()
+    rhs = w.rhs()
+    cores = os.cpu_count() or 1
+    if threads_cap:
+        cores = min(cores, threads_cap)
+    # ranks must divide jz at every one of the 4 levels
+    nproc = 1
+    for p in range(cores, 0, -1):
+        if (w.jz // 8) % p == 0:
+            nproc = p
+            break
+    o = Oracle(x, y, z, islor=1, nproc=nproc)
+    t0 = time.perf_counter()
+    _, cyc, _, rr = o.multi(rhs, eps=1e-30, ficycle=cycles)
+    dt = (time.perf_counter() - t0) / cycles
+    ncyc = REF_CYCLES_TO_1E10.get(workload)
+    value = 1.0 / (dt * ncyc) if ncyc else None
+    return {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
+            "sample": (f"{cycles} V-cycle(s) of the restated reference solver (line SOR, "
+                       f"{nproc} emulated MPI ranks as threads) on the full {workload} grid: "
+                       f"{dt:.2f} s per V-cycle x {ncyc} V-cycles to 1e-10"),
+            "seconds_per_vcycle": dt}
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    steps, warm = args.steps, args.warmup
+    from oracle.oracle import Oracle
+    from ples_gb300 import synthetic as S
+    w = S.WORKLOADS[args.workload]
+    x, y, z = w.grid()
+    rhs = w.rhs()
+    cores = os.cpu_count() or 1
+    nproc = 1
+    for p in range(cores, 0, -1):
+        if (w.jz // 8) % p == 0:
+            nproc = p
+            break
+    o = Oracle(x, y, z, islor=1, nproc=nproc)
+    ncyc = REF_CYCLES_TO_1E10.get(args.workload)
+    times = []
+    for s in range(warm + steps):
+        t0 = time.perf_counter()
+        o.multi(rhs, eps=1e-30, ficycle=1)
+        if s >= warm:
+            times.append(time.perf_counter() - t0)
+    t_cycle = sum(times) / len(times)
+    value = 1.0 / (t_cycle * ncyc) if ncyc else None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": t_cycle * ncyc * 1e3 if ncyc else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": args.workload, "grid": f"{w.jx}x{w.jy}x{w.jz}", "cells": w.cells,
+                   "solver": "restated reference multi: line SOR (islor=1), omega 1.6, kss 5/10, 4 levels",
+                   "step": "one V-cycle per step, scaled by the V-cycles to 1e-10"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
+                         "sample": f"1 V-cycle per step, {nproc} emulated ranks, x {ncyc} V-cycles"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="channel_256x128x256")
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--smoother", type=int, default=0)
+    ap.add_argument("--nu", type=int, default=0)
+    ap.add_argument("--inner", type=int, default=0)
+    ap.add_argument("--omega", type=float, default=0.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+    from ples_gb300 import mg
+    from ples_gb300 import synthetic as S
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    w = S.WORKLOADS[args.workload]
+    x, y, z = w.grid()
+    rhs = w.rhs()
+    kw = dict(device=local, smoother=args.smoother, nu_pre=args.nu, nu_post=args.nu,
+              inner_cycles=args.inner, omega=args.omega)
+    m = mg.Multigrid(x, y, z, precision="mixed", **kw)
+    nfi = (w.jx + 2) * (w.jy + 2) * (w.jz + 2)
+    d_fi = torch.zeros(nfi, dtype=torch.float64, device="cuda")
+    d_rhs = torch.from_numpy(np.ascontiguousarray(rhs.ravel(order="F"))).cuda()
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def step():
+        d_fi.zero_()
+        return m.solve_device(d_fi.data_ptr(), d_rhs.data_ptr(), rel_tol=1e-10, max_cycles=200, stream=sh)
+
+    for _ in range(args.warmup):
+        st = step()
+    torch.cuda.synchronize()
+    if st["status"] != mg.OK:
+        raise RuntimeError(f"warm-up solve did not converge: {st}")
+    m.time_kernel("line", 1)
+    n0 = m.counters()["launches"]
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = []
+    for _ in range(args.steps):
+        stats.append(step())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    launches = m.counters()["launches"] - n0
+    kms, kn = m.kernel_time()
+    m.time_kernel(None)
+    if dist:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = args.steps * ws / t
+    ms_per_step = t / args.steps * 1e3
+    outer = statistics.mean(s["outer_iterations"] for s in stats)
+    relres = max(s["rel_residual"] for s in stats)
+
+    # plain FP64 on the same grid
+    m64 = mg.Multigrid(x, y, z, precision="fp64", device=local, smoother=args.smoother,
+                       nu_pre=args.nu, nu_post=args.nu, inner_cycles=args.inner, omega=args.omega)
+    d_fi64 = torch.zeros(nfi, dtype=torch.float64, device="cuda")
+
+    def step64():
+        d_fi64.zero_()
+        return m64.solve_device(d_fi64.data_ptr(), d_rhs.data_ptr(), rel_tol=1e-10, max_cycles=400,
+                                stream=sh)
+
+    st64 = step64()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.fp64_steps):
+        st64 = step64()
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t64 = f0.elapsed_time(f1) / 1e3 / args.fp64_steps
+    # mixed vs FP64 solution agreement (zero-mean fields)
+    a = d_fi.cpu().numpy().reshape((w.jx + 2, w.jy + 2, w.jz + 2), order="F")[1:-1, 1:-1, 1:-1]
+    b = d_fi64.cpu().numpy().reshape((w.jx + 2, w.jy + 2, w.jz + 2), order="F")[1:-1, 1:-1, 1:-1]
+    err_vs_fp64 = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    del m64, d_fi64
+
+    # end to end through the host-buffer entry point with pinned buffers
+    h_fi = torch.zeros(nfi, dtype=torch.float64).pin_memory()
+    h_rhs = torch.from_numpy(np.ascontiguousarray(rhs.ravel(order="F"))).pin_memory()
+    fi_np = h_fi.numpy().reshape((w.jx + 2, w.jy + 2, w.jz + 2), order="F")
+    rhs_np = h_rhs.numpy().reshape((w.jx, w.jy, w.jz), order="F")
+    import ctypes as C
+    lib = mg.load()
+    stx = mg.Stats()
+
+    def step_e2e():
+        fi_np[...] = 0.0
+        rc = lib.ples_mg_solve(m._h, fi_np, rhs_np, None, 1e-10, 0.0, 200, C.byref(stx))
+        if rc != mg.OK:
+            raise RuntimeError(f"e2e solve failed: {rc}")
+
+    step_e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    te = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_value = ws / te  # every replica runs its own
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = _peaks()
+    cells = w.cells
+    avg_launch_s = kms / 1e3 / kn if kn else None
+    achieved = LINE_BYTES_PER_CELL * cells / avg_launch_s / 1e9 if avg_launch_s else None
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"line_relax_{args.workload}.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded wavy-wall channel grid and divergence RHS)",
+        "config": {"workload": args.workload, "grid": f"{w.jx}x{w.jy}x{w.jz}", "cells": cells,
+                   "wall_amplitude": w.amp, "y_stretch": w.beta, "rhs_seed": w.seed,
+                   "precision": "mixed: FP32 V-cycle, FP64 residual/update/projection",
+                   "tolerance": "||r||2/||b||2 <= 1e-10", "parallelism": f"replicas x{ws}",
+                   "l2": "inputs larger than L2 (no flush)", "levels": m.nlevel,
+                   "outer_iterations_mean": outer, "max_rel_residual": relres},
+        "fp64": {"value": 1.0 / t64, "unit": UNIT, "ms_per_solve": t64 * 1e3,
+                 "outer_iterations": st64["outer_iterations"]},
+        "mixed_over_fp64": (1.0 / t64) and value / ws / (1.0 / t64),
+        "err_mixed_vs_fp64": err_vs_fp64,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * (nfi + cells), "d2h_bytes_per_step": 8 * nfi},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": traffic,
+                     "kernel": "k_line_relax<float> level 1",
+                     "launches_timed": kn, "avg_launch_ms": avg_launch_s * 1e3 if avg_launch_s else None,
+                     "peak_source": peak_kind,
+                     "bytes_per_launch": LINE_BYTES_PER_CELL * cells},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,152 @@
+/*
+ * ples_mg.h -- C ABI of the GB300 pressure-Poisson multigrid.
+ *
+ * Drop-in for the pressure solve of PLES: the Fortran subroutine `multi`
+ * (fsrc/multigrid.f03:42-48, called at fsrc/stratiParticle.f03:2881-2887)
+ * and its set-up chain metrica -> mul_met -> wall (fsrc/stratiParticle.f03:
+ * 767-769).  Arrays cross the boundary as plain pointers to caller-owned,
+ * column-major FP64 buffers with the reference's lower bounds; no C++ or
+ * CUDA types appear in the signatures, so the functions bind directly from
+ * Fortran through iso_c_binding.
+ *
+ * Threading: one handle per host thread.  Every entry point returns a status
+ * code (PLES_MG_OK == 0); the handle also keeps the last error message.
+ */
+#ifndef PLES_MG_H
+#define PLES_MG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLES_MG_ABI_VERSION 1
+
+/* status codes */
+enum {
+    PLES_MG_OK = 0,
+    PLES_MG_NOT_CONVERGED = 1, /* max_cycles reached above tolerance        */
+    PLES_MG_BAD_ARG = 2,       /* invalid descriptor, size or pointer       */
+    PLES_MG_OOM = 3,           /* device allocation or HBM budget exceeded  */
+    PLES_MG_DEVICE_TIMEOUT = 4,/* a bounded device wait gave up             */
+    PLES_MG_CUDA_ERROR = 5,    /* CUDA runtime error                        */
+    PLES_MG_DIVERGED = 6,      /* NaN/Inf or residual growth                */
+    PLES_MG_NO_DEVICE = 7      /* no usable CUDA device                     */
+};
+
+/* inner-solve precision */
+enum {
+    PLES_MG_PREC_FP64 = 0,  /* plain: every kernel in FP64                          */
+    PLES_MG_PREC_MIXED = 1  /* FP32 V-cycle inside an FP64 defect-correction loop   */
+};
+
+/* layout of the node coordinates in the descriptor */
+enum {
+    PLES_MG_COORDS_NODES = 0,    /* x,y,z(0:jx, 0:jy, 0:jz)                         */
+    PLES_MG_COORDS_GHOSTED8 = 1  /* x,y,z(-8:jx+8, -8:jy+8, -8:jz+8), the single-   */
+                                 /* domain extent of myarrays_metri3 (iniz_metrica) */
+};
+
+/* ghost-layer fill rules, fsrc/multigrid.f03:1013-1936 */
+typedef struct {
+    int jx, jy, jz;        /* fine cells (scala3 jx, jy, jz)                        */
+    int ip, jp, kp;        /* 0 periodic, 1 wall (module period, Aboundary.in:6-8);
+                              jp must be 1 (multigrid.f03:1744-1746)                */
+    int nlevmax;           /* maximum multigrid levels; 0 = as many as the grid allows */
+    double omega;          /* relaxation factor of the line smoother (0 = default)   */
+    int precision;         /* PLES_MG_PREC_*                                        */
+    int coords_layout;     /* PLES_MG_COORDS_*                                      */
+    const double *x, *y, *z; /* host node coordinates, column-major                 */
+    double dt;             /* time step dividing the cs1..cs6 wall fluxes           */
+    int device;            /* CUDA device ordinal                                   */
+    int nu_pre, nu_post;   /* smoothing sweeps per level (0 = default)              */
+    int nu_coarse;         /* sweeps on the coarsest level (0 = default)            */
+    int inner_cycles;      /* V-cycles per outer FP64 iteration (0 = default)       */
+    int smoother;          /* 0 = eta-line Jacobi, 1 = 4-colour zebra eta-line SOR  */
+} ples_mg_desc;
+
+typedef struct {
+    int outer_iterations;   /* FP64 residual evaluations after the first           */
+    int vcycles;            /* inner V-cycles run                                   */
+    double rel_residual;    /* ||r||_2 / ||b||_2 of the returned solution           */
+    double max_residual;    /* max |r| of the returned solution                     */
+    double rhs_norm;        /* ||b||_2 after the compatibility projection          */
+    double rhs_mean_removed;/* mean subtracted from b (compatibility)               */
+    double seconds;         /* wall time of the call                                */
+    int status;
+} ples_mg_stats;
+
+typedef struct ples_mg_handle ples_mg_handle;
+
+/* Build the coefficient hierarchy on the device and keep it resident.
+ * Replaces metrica (fsrc/metrica.f03:2-501), cellep (fsrc/cellep.f03),
+ * indy (fsrc/indy.f03), mul_met (fsrc/multigrid.f03:2293-3052) and
+ * wall/sett (fsrc/multigrid.f03:3151-3264, fsrc/sett.f03). */
+int ples_mg_create(const ples_mg_desc *desc, ples_mg_handle **out);
+
+/* Replaces multi (fsrc/multigrid.f03:42-653).
+ *   fi  : in/out (0:jx+1, 0:jy+1, 0:jz+1); initial guess, returned solution
+ *         with its ghost layer filled (periodic copies and wall relations).
+ *   rhs : (1:jx, 1:jy, 1:jz) (fsrc/diver.f03); made compatible by removing
+ *         its mean net of the wall fluxes.
+ *   cs  : cs1..cs6 wall fluxes (myarrays_velo3): cs1,cs2 (1:jy,1:jz),
+ *         cs3,cs4 (1:jx,1:jz), cs5,cs6 (1:jx,1:jy); NULL = all zero.
+ *   Stops when ||r||_2/||b||_2 <= rel_tol (if rel_tol > 0) or
+ *   max|r| < abs_tol_max (if abs_tol_max > 0, the reference's eps test,
+ *   multigrid.f03:598-631), or after max_cycles outer iterations
+ *   (the reference's ficycle).  The solution is returned with zero mean. */
+int ples_mg_solve(ples_mg_handle *h, double *fi, const double *rhs,
+                  const double *const cs[6], double rel_tol,
+                  double abs_tol_max, int max_cycles, ples_mg_stats *stats);
+
+/* Same, on device-resident buffers with the same extents (column-major,
+ * FP64): no host copies.  stream is a cudaStream_t or NULL. */
+int ples_mg_solve_device(ples_mg_handle *h, double *d_fi, const double *d_rhs,
+                         const double *const d_cs[6], double rel_tol,
+                         double abs_tol_max, int max_cycles, void *stream,
+                         ples_mg_stats *stats);
+
+void ples_mg_destroy(ples_mg_handle *h);
+const char *ples_mg_strerror(int code);
+const char *ples_mg_last_error(const ples_mg_handle *h);
+
+/* ---- per-level operators (the hot-path routines one by one) --------- */
+int ples_mg_levels(const ples_mg_handle *h, int *nlevel);
+int ples_mg_level_dims(const ples_mg_handle *h, int level, int *nx, int *ny,
+                       int *nz);
+/* FP64 face metric of a level as built on the device, reference extents:
+ * which 0..8 = g11..g33 (before any scaling): g1* (0:nx,1:ny,1:nz),
+ * g2* (1:nx,0:ny,1:nz), g3* (1:nx,1:ny,0:nz).  Replaces the arrays of
+ * metrica (level 1) and mul_met (levels >= 2). */
+int ples_mg_get_metric(ples_mg_handle *h, int level, int which, double *out);
+/* rh1 = L_n(pr) - rh on the device (resid_sndrcv.f03:2-156);
+ * pr (0:nx+1,0:ny+1,0:nz+1), rh/out (1:nx,1:ny,1:nz).  precision selects
+ * the FP64 or the FP32 kernel. */
+int ples_mg_apply_residual(ples_mg_handle *h, int level, const double *pr,
+                           const double *rh, double *out, int precision);
+/* Ghost layer of pr at level `level` driven to the fixed point of the
+ * reference's fill (mul_boun_sndrcv, multigrid.f03:1013-1936): `passes`
+ * Jacobi passes; cs (level 1 only) as in ples_mg_solve. */
+int ples_mg_apply_ghost_fill(ples_mg_handle *h, int level, double *pr,
+                             const double *const cs[6], int passes);
+/* out = restriction of rh (restrict_sndrcv.f03:2-56), level -> level+1 */
+int ples_mg_apply_restrict(ples_mg_handle *h, int level, const double *rh,
+                           double *out);
+/* prf += prolongation of prc (prolong.f03:2-261), level+1 -> level */
+int ples_mg_apply_prolong(ples_mg_handle *h, int level, double *prf,
+                          const double *prc);
+
+/* ---- instrumentation (the reference's only instrument is the wall-clock
+ * mlt timer around multi, fsrc/stratiParticle.f03:2874,2921-2927) ------- */
+/* kernels launched on the device by this handle so far, and its resident
+ * device bytes */
+int ples_mg_counters(ples_mg_handle *h, long long *launches, long long *device_bytes);
+/* time one kernel kind at one level with CUDA events on the solve stream:
+ * kind 0 eta-line smoother, 1 residual+restriction, 2 prolongation,
+ * 3 FP64 outer residual; kind -1 switches timing off.  Resets the totals. */
+int ples_mg_kernel_timing(ples_mg_handle *h, int kind, int level);
+int ples_mg_kernel_time(ples_mg_handle *h, double *total_ms, long long *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PLES_MG_H */

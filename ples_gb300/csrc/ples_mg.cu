@@ -1,0 +1,1154 @@
+// ples_mg.cu -- the GB300 pressure-Poisson multigrid behind include/ples_mg.h.
+//
+// Solve structure (replaces multi, fsrc/multigrid.f03:42-653):
+//   FP64 outer defect correction on the fine level
+//     x      : FP64 solution box (the caller's fi with its ghost layer)
+//     r      = b - L(x)            FP64, with its norm (stop test)
+//     e      ~ L^-1 r              inner V-cycle(s) in FP32 (mixed) or FP64
+//     x     += e
+//   inner V-cycle over levels 1..L: eta-line smoothing, residual+restriction,
+//   prolongation; coarse operators from sub-sampled nodes (mul_met).
+// The ghost layer of x is driven to the fixed point of the reference's fill
+// before every outer residual; the compatibility projection removes the
+// mean of b net of the wall fluxes and the returned solution has zero mean.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mg_device.cuh"
+#include "metric.h"
+#include "ples_mg.h"
+
+using namespace ples;
+
+namespace {
+
+constexpr int kMaxLev = 12;
+constexpr int kRedThreads = 256;
+
+// ---------------------------------------------------------------------------
+// kernels of the outer loop, reductions and layout conversion
+
+template <typename T>
+__global__ void k_scale_coef(long long n, const double* __restrict__ g11, const double* __restrict__ g12,
+                             const double* __restrict__ g13, const double* __restrict__ g21,
+                             const double* __restrict__ g22, const double* __restrict__ g23,
+                             const double* __restrict__ g31, const double* __restrict__ g32,
+                             const double* __restrict__ g33, Coef<T> o, double ppot2) {
+    const double pq = ppot2 * 0.25;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        o.a1[q] = T(g11[q] * ppot2); o.b12[q] = T(g12[q] * pq); o.b13[q] = T(g13[q] * pq);
+        o.a2[q] = T(g22[q] * ppot2); o.b21[q] = T(g21[q] * pq); o.b23[q] = T(g23[q] * pq);
+        o.a3[q] = T(g33[q] * ppot2); o.b31[q] = T(g31[q] * pq); o.b32[q] = T(g32[q] * pq);
+    }
+}
+
+__device__ __forceinline__ void block_reduce_sum_max(double& s, double& m) {
+    __shared__ double ss[32], sm[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    if (lane == 0) { ss[w] = s; sm[w] = m; }
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    if (w == 0) {
+        s = lane < nw ? ss[lane] : 0.0;
+        m = lane < nw ? sm[lane] : 0.0;
+        for (int o = 16; o; o >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        }
+    }
+}
+
+// r = b - L(x) on the fine level in FP64 (resid_sndrcv with the sign of the
+// inner right-hand side), stored in the inner precision; per-block partial
+// sum of squares and max |r| (multigrid.f03:595-631).
+template <typename Ti>
+__global__ void k_resid_outer(Geom g, Coef<double> c, const double* __restrict__ x, const double* __restrict__ b,
+                              Ti* __restrict__ rin, double* __restrict__ psq, double* __restrict__ pmax) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + tx + 1;
+    const int j = blockIdx.y * (kRedThreads / 32) + ty + 1;
+    const int k = blockIdx.z + 1;
+    double s = 0.0, m = 0.0;
+    if (i <= g.nx && j <= g.ny) {
+        const long long q = g.at(i, j, k);
+        const double r = -cell_residual(g, c, x, b, q);
+        rin[q] = Ti(r);
+        s = r * r;
+        m = fabs(r);
+    }
+    // NaN must survive the max: fmax drops NaN, so carry it in the sum
+    block_reduce_sum_max(s, m);
+    if (threadIdx.x == 0) {
+        const long long blk = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        psq[blk] = s;
+        pmax[blk] = m;
+    }
+}
+
+// sum / sum of squares of interior cells, per-block partials
+__global__ void k_sum_interior(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + tx + 1;
+    const int j = blockIdx.y * (kRedThreads / 32) + ty + 1;
+    const int k = blockIdx.z + 1;
+    double s = 0.0, m = 0.0;
+    if (i <= g.nx && j <= g.ny) {
+        const double v = a[g.at(i, j, k)];
+        s = squares ? v * v : v;
+    }
+    block_reduce_sum_max(s, m);
+    if (threadIdx.x == 0)
+        psum[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s;
+}
+
+// deterministic final reduction of n partials (sum of a, max of bmax)
+__global__ void k_reduce_final(const double* __restrict__ a, const double* __restrict__ bmax, long long n,
+                               double* __restrict__ out) {
+    double s = 0.0, m = 0.0;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+        s += a[t];
+        if (bmax) m = fmax(m, bmax[t]);
+    }
+    block_reduce_sum_max(s, m);
+    if (threadIdx.x == 0) { out[0] = s; out[1] = m; }
+}
+
+__global__ void k_add_interior(Geom g, double* __restrict__ a, double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i <= g.nx && j <= g.ny) a[g.at(i, j, k)] += v;
+}
+
+__global__ void k_add_box(Geom g, double* __restrict__ a, double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i <= g.nx + 1 && j <= g.ny + 1) a[g.at(i, j, k)] += v;
+}
+
+template <typename Te>
+__global__ void k_update(Geom g, double* __restrict__ x, const Te* __restrict__ e) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i <= g.nx + 1 && j <= g.ny + 1) {
+        const long long q = g.at(i, j, k);
+        x[q] += double(e[q]);
+    }
+}
+
+// FP64 wall ghost rows j = 0 and ny+1 from the current field
+// (mul_boun_sndrcv, multigrid.f03:1160-1186, freesurface = 0), written to a
+// side buffer so that one pass is a Jacobi step (race-free, deterministic).
+__global__ void k_wall_compute(Geom g, Coef<double> c, const double* __restrict__ p, double* __restrict__ w,
+                               const double* __restrict__ cs3, const double* __restrict__ cs4, double an_dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int side = blockIdx.z;
+    if (i > g.nx || k > g.nz) return;
+    const long long sj = g.sj, sk = g.sk;
+    const long long widx = (long long)side * g.nx * g.nz + (long long)(k - 1) * g.nx + (i - 1);
+    if (side == 0) {
+        const long long q0 = g.at(i, 0, k), q1 = q0 + sj;
+        const double a2 = c.a2[q0];
+        double v = p[q1];
+        if (cs3) v -= an_dt * cs3[(long long)(k - 1) * g.nx + (i - 1)] / a2;
+        v += (c.b21[q0] * (p[q1 + 1] + p[q0 + 1] - p[q1 - 1] - p[q0 - 1]) +
+              c.b23[q0] * (p[q1 + sk] + p[q0 + sk] - p[q1 - sk] - p[q0 - sk])) / a2;
+        w[widx] = v;
+    } else {
+        const long long qt = g.at(i, g.ny + 1, k), qn = qt - sj;
+        const double a2 = c.a2[qn];
+        double v = p[qn];
+        if (cs4) v += an_dt * cs4[(long long)(k - 1) * g.nx + (i - 1)] / a2;
+        v -= (c.b21[qn] * (p[qt + 1] + p[qn + 1] - p[qt - 1] - p[qn - 1]) +
+              c.b23[qn] * (p[qt + sk] + p[qn + sk] - p[qt - sk] - p[qn - sk])) / a2;
+        w[widx] = v;
+    }
+}
+
+// scatter the wall rows, including their periodic x/z images (edges and
+// corners of the ghost shell)
+__global__ void k_wall_scatter(Geom g, double* __restrict__ p, const double* __restrict__ w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.y * blockDim.y + threadIdx.y;
+    const int side = blockIdx.z;
+    if (i > g.nx + 1 || k > g.nz + 1) return;
+    const int wi = i == 0 ? g.nx : (i == g.nx + 1 ? 1 : i);
+    const int wk = k == 0 ? g.nz : (k == g.nz + 1 ? 1 : k);
+    p[g.at(i, side ? g.ny + 1 : 0, k)] = w[(long long)side * g.nx * g.nz + (long long)(wk - 1) * g.nx + (wi - 1)];
+}
+
+// contraction factor of the Jacobi wall fill: max 2(|B21|+|B23|)/A2
+__global__ void k_wall_contraction(Geom g, Coef<double> c, unsigned long long* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > g.nx || k > g.nz) return;
+    const long long q0 = g.at(i, 0, k), qn = g.at(i, g.ny, k);
+    double v = fmax(2.0 * (fabs(c.b21[q0]) + fabs(c.b23[q0])) / c.a2[q0],
+                    2.0 * (fabs(c.b21[qn]) + fabs(c.b23[qn])) / c.a2[qn]);
+    atomicMax(out, (unsigned long long)__double_as_longlong(v));
+}
+
+// compact Fortran arrays <-> ghosted boxes
+__global__ void k_compact_to_box(Geom g, int ghost, const double* __restrict__ src, double* __restrict__ dst) {
+    const int o = ghost ? 0 : 1;
+    const int ex = ghost ? g.nx + 2 : g.nx, ey = ghost ? g.ny + 2 : g.ny, ez = ghost ? g.nz + 2 : g.nz;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y * blockDim.y + threadIdx.y;
+    const int c = blockIdx.z;
+    if (a >= ex || b >= ey) return;
+    dst[g.at(a + o, b + o, c + o)] = src[((long long)c * ey + b) * ex + a];
+    (void)ez;
+}
+
+__global__ void k_box_to_compact(Geom g, int ghost, const double* __restrict__ src, double* __restrict__ dst) {
+    const int o = ghost ? 0 : 1;
+    const int ex = ghost ? g.nx + 2 : g.nx, ey = ghost ? g.ny + 2 : g.ny;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y * blockDim.y + threadIdx.y;
+    const int c = blockIdx.z;
+    if (a >= ex || b >= ey) return;
+    dst[((long long)c * ey + b) * ex + a] = src[g.at(a + o, b + o, c + o)];
+}
+
+// face arrays with the reference extents: (i0:i1, j0:j1, k0:k1) of a box
+__global__ void k_box_extract(Geom g, const double* __restrict__ src, int i0, int i1, int j0, int j1, int k0,
+                              double* __restrict__ dst) {
+    const int ex = i1 - i0 + 1, ey = j1 - j0 + 1;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y * blockDim.y + threadIdx.y;
+    const int c = blockIdx.z;
+    if (a >= ex || b >= ey) return;
+    dst[((long long)c * ey + b) * ex + a] = src[g.at(a + i0, b + j0, c + k0)];
+}
+
+template <typename To, typename Ti>
+__global__ void k_convert(long long n, const Ti* __restrict__ a, To* __restrict__ b) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x)
+        b[q] = To(a[q]);
+}
+
+// ---------------------------------------------------------------------------
+inline int grid1(long long n, int t = 256) {
+    long long b = (n + t - 1) / t;
+    return (int)(b < 4096 ? (b < 1 ? 1 : b) : 4096);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct LevelData {
+    Geom g;
+    void* p = nullptr;   // inner-precision fields (T boxes)
+    void* p2 = nullptr;
+    void* rh = nullptr;
+    Coef<float> cf{};     // FP32 scaled coefficients (mixed)
+    Coef<double> cd{};    // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
+    bool has_cf = false, has_cd = false;
+};
+
+struct ples_mg_handle {
+    ples_mg_desc d{};
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    int nlev = 0;
+    LevelData L[kMaxLev];
+    double *xn = nullptr, *yn = nullptr, *zn = nullptr;  // fine nodes (0:jx,0:jy,0:jz)
+    double *x = nullptr, *b = nullptr;                   // FP64 solution / rhs boxes (level 1)
+    double* wbuf = nullptr;                              // 2*nx*nz wall rows
+    double *part_a = nullptr, *part_b = nullptr;         // block partials
+    long long npart = 0;
+    double* red = nullptr;                               // 2 doubles on the device
+    double* h_red = nullptr;                             // pinned host copy
+    double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
+    double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes
+    double* cs_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // their device buffers
+    int wall_passes = 3;
+    double wall_q = 0.0;
+    int nu_pre = 2, nu_post = 2, nu_coarse = 40, inner_cycles = 1, smoother = 0;
+    double omega = 0.8;
+    std::vector<void*> allocs;
+    std::string err;
+    long long bytes = 0;
+    // instrumentation: kernels launched, and optional CUDA-event timing of
+    // one kernel kind at one level (pairs are read back after each solve)
+    long long launches = 0;
+    int timed_kind = -1, timed_level = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    double timed_ms = 0.0;
+    long long timed_launches = 0;
+};
+
+namespace {
+
+int fail(ples_mg_handle* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                               \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? PLES_MG_OOM : PLES_MG_CUDA_ERROR, \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                       \
+    } while (0)
+
+// kernel kinds for the optional event timing
+enum { KIND_LINE = 0, KIND_RESTRICT = 1, KIND_PROLONG = 2, KIND_OUTER = 3, KIND_GHOST = 4, KIND_WALL = 5 };
+
+void timed_begin(ples_mg_handle* h, int kind, int level) {
+    if (h->timed_kind != kind || h->timed_level != level) return;
+    if (h->ev_used + 2 > h->ev_pool.size()) {
+        for (int q = 0; q < 64; ++q) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            h->ev_pool.push_back(e);
+        }
+    }
+    cudaEventRecord(h->ev_pool[h->ev_used], h->st);
+}
+void timed_end(ples_mg_handle* h, int kind, int level) {
+    if (h->timed_kind != kind || h->timed_level != level) return;
+    cudaEventRecord(h->ev_pool[h->ev_used + 1], h->st);
+    h->ev_used += 2;
+}
+// after a stream synchronisation: fold recorded pairs into the totals
+void timed_collect(ples_mg_handle* h) {
+    for (size_t q = 0; q + 1 < h->ev_used; q += 2) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->ev_pool[q], h->ev_pool[q + 1]) == cudaSuccess) {
+            h->timed_ms += ms;
+            h->timed_launches += 1;
+        }
+    }
+    h->ev_used = 0;
+}
+
+int dalloc(ples_mg_handle* h, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, PLES_MG_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    h->allocs.push_back(*p);
+    h->bytes += (long long)bytes;
+    e = cudaMemsetAsync(*p, 0, bytes, h->st);
+    if (e != cudaSuccess) return fail(h, PLES_MG_CUDA_ERROR, "cudaMemset failed: %s", cudaGetErrorString(e));
+    return PLES_MG_OK;
+}
+
+template <typename T>
+int alloc_coef(ples_mg_handle* h, const Geom& g, Coef<T>& c) {
+    T** f[9] = {&c.a1, &c.b12, &c.b13, &c.a2, &c.b21, &c.b23, &c.a3, &c.b31, &c.b32};
+    for (auto pp : f) {
+        int rc = dalloc(h, (void**)pp, sizeof(T) * (size_t)g.n);
+        if (rc) return rc;
+    }
+    return PLES_MG_OK;
+}
+
+void free_tmp(std::vector<void*>& v) {
+    for (void* p : v) cudaFree(p);
+    v.clear();
+}
+
+// raw FP64 metric of a level into 9 temporary boxes
+int raw_metric(ples_mg_handle* h, int lev, double* gout[9], std::vector<void*>& tmp) {
+    const Geom& g = h->L[lev - 1].g;
+    for (int c = 0; c < 9; ++c) {
+        cudaError_t e = cudaMalloc((void**)&gout[c], sizeof(double) * (size_t)g.n);
+        if (e != cudaSuccess) { free_tmp(tmp); return fail(h, PLES_MG_OOM, "metric scratch: %s", cudaGetErrorString(e)); }
+        tmp.push_back(gout[c]);
+        CK(cudaMemsetAsync(gout[c], 0, sizeof(double) * (size_t)g.n, h->st));
+    }
+    CK(launch_metric(h->xn, h->yn, h->zn, h->d.jx, h->d.jy, h->d.jz, h->d.ip, h->d.jp, h->d.kp, lev, g,
+                     gout, h->st));
+    return PLES_MG_OK;
+}
+
+template <typename T>
+int scale_into(ples_mg_handle* h, int lev, double* const gr[9], Coef<T>& c) {
+    const Geom& g = h->L[lev - 1].g;
+    const double ppot2 = std::ldexp(1.0, -2 * (lev - 1));
+    k_scale_coef<T><<<grid1(g.n), 256, 0, h->st>>>(g.n, gr[0], gr[1], gr[2], gr[3], gr[4], gr[5], gr[6], gr[7],
+                                                   gr[8], c, ppot2);
+    CK(cudaGetLastError());
+    return PLES_MG_OK;
+}
+
+// ---- inner V-cycle ----------------------------------------------------------
+template <typename T>
+Coef<T> coef_of(LevelData& L);
+template <>
+Coef<float> coef_of<float>(LevelData& L) { return L.cf; }
+template <>
+Coef<double> coef_of<double>(LevelData& L) { return L.cd; }
+
+template <typename T>
+void ghost_xz(ples_mg_handle* h, const Geom& g, T* p) {
+    const long long tot = 2LL * (g.nx + 2) * (g.ny + 2) + 2LL * (g.ny + 2) * g.nz;
+    k_ghost_xz<T><<<grid1(tot), 256, 0, h->st>>>(g, p);
+    ++h->launches;
+}
+
+template <typename T>
+int line_block(const Geom& g, dim3& blk, size_t& smem) {
+    const size_t per = 2 * (size_t)(g.ny + 2) * 32 * sizeof(T);
+    int ty = (int)(72 * 1024 / per);
+    if (ty > 4) ty = 4;
+    if (ty < 1) ty = 1;
+    blk = dim3(32, ty);
+    smem = per * ty;
+    return smem <= 200 * 1024 ? 0 : -1;
+}
+
+// the dynamic shared-memory limit is a per-function attribute shared by all
+// handles of the process: only ever raise it
+template <typename T>
+int set_smem_attrs(ples_mg_handle* h, size_t smem) {
+    static size_t current = 0;
+    if (smem <= current) return 0;
+    current = smem;
+    CK(cudaFuncSetAttribute(k_line_relax<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return 0;
+}
+
+template <typename T>
+void smooth(ples_mg_handle* h, LevelData& L, int nu, int level) {
+    dim3 blk;
+    size_t smem;
+    line_block<T>(L.g, blk, smem);
+    Coef<T> c = coef_of<T>(L);
+    const T om = T(h->omega);
+    for (int s = 0; s < nu; ++s) {
+        if (h->smoother == 0) {
+            ghost_xz<T>(h, L.g, (T*)L.p);
+            dim3 grd((L.g.nx + 31) / 32, (L.g.nz + blk.y - 1) / blk.y);
+            timed_begin(h, KIND_LINE, level);
+            k_line_relax<T, false><<<grd, blk, smem, h->st>>>(L.g, c, (const T*)L.p, (T*)L.p2,
+                                                              (const T*)L.rh, om, 0);
+            timed_end(h, KIND_LINE, level);
+            ++h->launches;
+            std::swap(L.p, L.p2);
+        } else {
+            dim3 grd((L.g.nx / 2 + 31) / 32, (L.g.nz / 2 + blk.y - 1) / blk.y);
+            for (int colour = 0; colour < 4; ++colour) {
+                ghost_xz<T>(h, L.g, (T*)L.p);
+                timed_begin(h, KIND_LINE, level);
+                k_line_relax<T, true><<<grd, blk, smem, h->st>>>(L.g, c, (const T*)L.p, (T*)L.p,
+                                                                 (const T*)L.rh, om, colour);
+                timed_end(h, KIND_LINE, level);
+                ++h->launches;
+            }
+        }
+    }
+}
+
+template <typename T>
+void vcycle(ples_mg_handle* h) {
+    const int nl = h->nlev;
+    for (int n = 0; n < nl - 1; ++n) {
+        LevelData& F = h->L[n];
+        LevelData& C = h->L[n + 1];
+        smooth<T>(h, F, h->nu_pre, n + 1);
+        ghost_xz<T>(h, F.g, (T*)F.p);
+        dim3 blk(32, 4), grd((C.g.nx + 31) / 32, (C.g.ny + 3) / 4, C.g.nz);
+        timed_begin(h, KIND_RESTRICT, n + 1);
+        k_resid_restrict<T><<<grd, blk, 0, h->st>>>(F.g, C.g, coef_of<T>(F), (const T*)F.p, (const T*)F.rh,
+                                                    (T*)C.rh);
+        timed_end(h, KIND_RESTRICT, n + 1);
+        ++h->launches;
+        cudaMemsetAsync(C.p, 0, sizeof(T) * (size_t)C.g.n, h->st);
+    }
+    smooth<T>(h, h->L[nl - 1], h->nu_coarse, nl);
+    for (int n = nl - 2; n >= 0; --n) {
+        LevelData& F = h->L[n];
+        LevelData& C = h->L[n + 1];
+        ghost_xz<T>(h, C.g, (T*)C.p);
+        dim3 blk(32, 4), grd((C.g.nx + 1 + 31) / 32, (C.g.ny + 1 + 3) / 4, C.g.nz + 1);
+        timed_begin(h, KIND_PROLONG, n + 1);
+        k_prolong<T, T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p);
+        timed_end(h, KIND_PROLONG, n + 1);
+        ++h->launches;
+        smooth<T>(h, F, h->nu_post, n + 1);
+    }
+}
+
+// ---- outer loop pieces ---------------------------------------------------------
+int reduce_to_host(ples_mg_handle* h, const double* a, const double* bmax, long long n, double out[2]) {
+    k_reduce_final<<<1, 1024, 0, h->st>>>(a, bmax, n, h->red);
+    ++h->launches;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_red, h->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    timed_collect(h);
+    out[0] = h->h_red[0];
+    out[1] = h->h_red[1];
+    return PLES_MG_OK;
+}
+
+dim3 red_grid(const Geom& g) { return dim3((g.nx + 31) / 32, (g.ny + kRedThreads / 32 - 1) / (kRedThreads / 32), g.nz); }
+
+int sum_interior(ples_mg_handle* h, const double* a, int squares, double* out) {
+    const Geom& g = h->L[0].g;
+    dim3 grd = red_grid(g);
+    k_sum_interior<<<grd, kRedThreads, 0, h->st>>>(g, a, squares, h->part_a);
+    ++h->launches;
+    CK(cudaGetLastError());
+    double r[2];
+    int rc = reduce_to_host(h, h->part_a, nullptr, (long long)grd.x * grd.y * grd.z, r);
+    *out = r[0];
+    return rc;
+}
+
+void wall_fill(ples_mg_handle* h, double* p, const double* cs3, const double* cs4, double an_dt, int passes,
+               const Geom& g, const Coef<double>& c) {
+    ghost_xz<double>(h, g, p);
+    dim3 blk(32, 4);
+    for (int s = 0; s < passes; ++s) {
+        k_wall_compute<<<dim3((g.nx + 31) / 32, (g.nz + 3) / 4, 2), blk, 0, h->st>>>(g, c, p, h->wbuf, cs3, cs4,
+                                                                                    an_dt);
+        k_wall_scatter<<<dim3((g.nx + 2 + 31) / 32, (g.nz + 2 + 3) / 4, 2), blk, 0, h->st>>>(g, p, h->wbuf);
+        h->launches += 2;
+    }
+}
+
+dim3 box_grid(const Geom& g) { return dim3((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2); }
+
+template <typename T>
+int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles, ples_mg_stats* st) {
+    LevelData& F = h->L[0];
+    const Geom& g = F.g;
+    const double N = (double)g.nx * g.ny * g.nz;
+    const double dt = h->d.dt;
+    // compatibility: sum(b) must equal the net wall flux (cs4 - cs3)/dt
+    double sb = 0.0;
+    int rc = sum_interior(h, h->b, 0, &sb);
+    if (rc) return rc;
+    double flux = 0.0;
+    if (h->cs_c[2] || h->cs_c[3]) {
+        double s3 = 0.0, s4 = 0.0;
+        // wall flux sums: reuse the reduction on the compact arrays
+        for (int side = 0; side < 2; ++side) {
+            const double* a = h->cs_c[2 + side];
+            if (!a) continue;
+            long long n = (long long)g.nx * g.nz;
+            k_reduce_final<<<1, 1024, 0, h->st>>>(a, nullptr, n, h->red);
+            ++h->launches;
+            CK(cudaMemcpyAsync(h->h_red, h->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
+            (side ? s4 : s3) = h->h_red[0];
+        }
+        flux = (s4 - s3) / dt;
+    }
+    const double shift = (sb - flux) / N;
+    {
+        dim3 blk(32, 4), grd((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
+        k_add_interior<<<grd, blk, 0, h->st>>>(g, h->b, -shift);
+        ++h->launches;
+    }
+    double bn2 = 0.0;
+    rc = sum_interior(h, h->b, 1, &bn2);
+    if (rc) return rc;
+    const double bnorm = bn2 > 0.0 ? std::sqrt(bn2) : 1.0;
+    st->rhs_norm = std::sqrt(bn2);
+    st->rhs_mean_removed = shift;
+
+    const dim3 rg = red_grid(g);
+    const long long nblk = (long long)rg.x * rg.y * rg.z;
+    double rel = 0.0, rmax = 0.0, rel0 = -1.0;
+    int it = 0, status = PLES_MG_NOT_CONVERGED, vcyc = 0;
+    for (;;) {
+        wall_fill(h, h->x, h->cs_c[2], h->cs_c[3], 1.0 / dt, h->wall_passes, g, F.cd);
+        timed_begin(h, KIND_OUTER, 1);
+        k_resid_outer<T><<<rg, kRedThreads, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b);
+        timed_end(h, KIND_OUTER, 1);
+        ++h->launches;
+        CK(cudaGetLastError());
+        double r2[2];
+        rc = reduce_to_host(h, h->part_a, h->part_b, nblk, r2);
+        if (rc) return rc;
+        rel = std::sqrt(r2[0]) / bnorm;
+        rmax = r2[1];
+        if (!std::isfinite(rel)) { status = PLES_MG_DIVERGED; break; }
+        if (rel0 < 0.0) rel0 = rel;
+        if ((rel_tol > 0.0 && rel <= rel_tol) || (abs_tol > 0.0 && rmax < abs_tol) || bn2 == 0.0) {
+            status = PLES_MG_OK;
+            break;
+        }
+        if (rel > 1e6 * rel0 && rel > 1.0) { status = PLES_MG_DIVERGED; break; }
+        if (it >= max_cycles) break;
+        CK(cudaMemsetAsync(F.p, 0, sizeof(T) * (size_t)g.n, h->st));
+        for (int c = 0; c < h->inner_cycles; ++c) {
+            vcycle<T>(h);
+            ++vcyc;
+        }
+        k_update<T><<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, (const T*)F.p);
+        ++h->launches;
+        CK(cudaGetLastError());
+        ++it;
+    }
+    // zero-mean solution (Neumann null space)
+    double sx = 0.0;
+    rc = sum_interior(h, h->x, 0, &sx);
+    if (rc) return rc;
+    k_add_box<<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, -sx / N);
+    ++h->launches;
+    CK(cudaGetLastError());
+    st->outer_iterations = it;
+    st->vcycles = vcyc;
+    st->rel_residual = rel;
+    st->max_residual = rmax;
+    st->status = status;
+    return status;
+}
+
+int validate(const ples_mg_desc* d, ples_mg_handle* h) {
+    if (!d) return fail(h, PLES_MG_BAD_ARG, "null descriptor");
+    if (d->jx < 8 || d->jy < 4 || d->jz < 8) return fail(h, PLES_MG_BAD_ARG, "grid too small (jx,jz >= 8, jy >= 4)");
+    if (d->jp != 1) return fail(h, PLES_MG_BAD_ARG, "y-periodic grids are not supported (jp must be 1)");
+    if (d->ip != 0 || d->kp != 0)
+        return fail(h, PLES_MG_BAD_ARG, "x or z walls (ip/kp = 1) are not supported on the device");
+    if (d->precision != PLES_MG_PREC_FP64 && d->precision != PLES_MG_PREC_MIXED)
+        return fail(h, PLES_MG_BAD_ARG, "unknown precision %d", d->precision);
+    if (d->coords_layout != PLES_MG_COORDS_NODES && d->coords_layout != PLES_MG_COORDS_GHOSTED8)
+        return fail(h, PLES_MG_BAD_ARG, "unknown coords_layout %d", d->coords_layout);
+    if (!d->x || !d->y || !d->z) return fail(h, PLES_MG_BAD_ARG, "null coordinate pointer");
+    if (!(d->dt > 0.0) || !std::isfinite(d->dt)) return fail(h, PLES_MG_BAD_ARG, "dt must be positive");
+    if (d->nlevmax < 0 || d->nu_pre < 0 || d->nu_post < 0 || d->nu_coarse < 0 || d->inner_cycles < 0)
+        return fail(h, PLES_MG_BAD_ARG, "negative level or sweep count");
+    if (d->smoother != 0 && d->smoother != 1) return fail(h, PLES_MG_BAD_ARG, "unknown smoother %d", d->smoother);
+    if (d->jx % 2 || d->jz % 2) return fail(h, PLES_MG_BAD_ARG, "jx and jz must be even");
+    return PLES_MG_OK;
+}
+
+int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
+    int rc = validate(d, h);
+    if (rc) return rc;
+    h->d = *d;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(h, PLES_MG_NO_DEVICE, "no CUDA device available");
+    if (d->device < 0 || d->device >= ndev) return fail(h, PLES_MG_BAD_ARG, "device %d out of range", d->device);
+    h->dev = d->device;
+    CK(cudaSetDevice(h->dev));
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    h->smoother = d->smoother;
+    h->omega = d->omega > 0.0 ? d->omega : (d->smoother == 0 ? 0.8 : 1.0);
+    h->nu_pre = d->nu_pre ? d->nu_pre : 2;
+    h->nu_post = d->nu_post ? d->nu_post : 2;
+    h->nu_coarse = d->nu_coarse ? d->nu_coarse : 40;
+    h->inner_cycles = d->inner_cycles ? d->inner_cycles : 1;
+    const int jx = d->jx, jy = d->jy, jz = d->jz;
+    // level sizes (indy.f03 halving; the level count is limited by the grid,
+    // not by the reference's 4-level arrays, because the coarse metric reads
+    // ghost nodes on the fly)
+    int nx = jx, ny = jy, nz = jz, nl = 1;
+    h->L[0].g = make_geom(nx, ny, nz);
+    const int cap = d->nlevmax > 0 ? d->nlevmax : kMaxLev;
+    while (nl < cap && nl < kMaxLev && nx % 2 == 0 && ny % 2 == 0 && nz % 2 == 0 && nx / 2 >= 4 && ny / 2 >= 2 &&
+           nz / 2 >= 4) {
+        nx /= 2; ny /= 2; nz /= 2;
+        h->L[nl].g = make_geom(nx, ny, nz);
+        ++nl;
+    }
+    h->nlev = nl;
+    // nodes
+    const size_t nn = (size_t)(jx + 1) * (jy + 1) * (jz + 1);
+    std::vector<double> hx, hy, hz;
+    const double *sx = d->x, *sy = d->y, *sz = d->z;
+    if (d->coords_layout == PLES_MG_COORDS_GHOSTED8) {
+        hx.resize(nn); hy.resize(nn); hz.resize(nn);
+        const long long ex = jx + 17, ey = jy + 17;
+        size_t q = 0;
+        for (int k = 0; k <= jz; ++k)
+            for (int j = 0; j <= jy; ++j)
+                for (int i = 0; i <= jx; ++i, ++q) {
+                    long long s = ((long long)(k + 8) * ey + (j + 8)) * ex + (i + 8);
+                    hx[q] = d->x[s]; hy[q] = d->y[s]; hz[q] = d->z[s];
+                }
+        sx = hx.data(); sy = hy.data(); sz = hz.data();
+    }
+    if ((rc = dalloc(h, (void**)&h->xn, nn * 8)) || (rc = dalloc(h, (void**)&h->yn, nn * 8)) ||
+        (rc = dalloc(h, (void**)&h->zn, nn * 8)))
+        return rc;
+    CK(cudaMemcpyAsync(h->xn, sx, nn * 8, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->yn, sy, nn * 8, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->zn, sz, nn * 8, cudaMemcpyHostToDevice, h->st));
+    // coefficients per level
+    const bool mixed = d->precision == PLES_MG_PREC_MIXED;
+    size_t smem_max = 0;
+    for (int n = 1; n <= nl; ++n) {
+        LevelData& L = h->L[n - 1];
+        double* gr[9];
+        std::vector<void*> tmp;
+        if ((rc = raw_metric(h, n, gr, tmp))) return rc;
+        if (n == 1 || !mixed) {
+            if ((rc = alloc_coef(h, L.g, L.cd)) || (rc = scale_into(h, n, gr, L.cd))) { free_tmp(tmp); return rc; }
+            L.has_cd = true;
+        }
+        if (mixed) {
+            if ((rc = alloc_coef(h, L.g, L.cf)) || (rc = scale_into(h, n, gr, L.cf))) { free_tmp(tmp); return rc; }
+            L.has_cf = true;
+        }
+        CK(cudaStreamSynchronize(h->st));
+        free_tmp(tmp);
+        const size_t es = mixed ? sizeof(float) : sizeof(double);
+        if ((rc = dalloc(h, &L.p, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.p2, es * (size_t)L.g.n)) ||
+            (rc = dalloc(h, &L.rh, es * (size_t)L.g.n)))
+            return rc;
+        dim3 blk;
+        size_t smem;
+        if (mixed ? line_block<float>(L.g, blk, smem) : line_block<double>(L.g, blk, smem))
+            return fail(h, PLES_MG_BAD_ARG, "eta lines too long for shared memory (jy = %d)", L.g.ny);
+        if (smem > smem_max) smem_max = smem;
+    }
+    if ((rc = mixed ? set_smem_attrs<float>(h, smem_max) : set_smem_attrs<double>(h, smem_max))) return rc;
+    const Geom& g = h->L[0].g;
+    if ((rc = dalloc(h, (void**)&h->x, 8 * (size_t)g.n)) || (rc = dalloc(h, (void**)&h->b, 8 * (size_t)g.n)) ||
+        (rc = dalloc(h, (void**)&h->wbuf, 8 * 2 * (size_t)g.nx * g.nz)))
+        return rc;
+    dim3 rg = red_grid(g);
+    h->npart = (long long)rg.x * rg.y * rg.z;
+    if ((rc = dalloc(h, (void**)&h->part_a, 8 * (size_t)h->npart)) ||
+        (rc = dalloc(h, (void**)&h->part_b, 8 * (size_t)h->npart)) || (rc = dalloc(h, (void**)&h->red, 64)))
+        return rc;
+    CK(cudaMallocHost((void**)&h->h_red, 64));
+    const size_t nfi = (size_t)(jx + 2) * (jy + 2) * (jz + 2), nrh = (size_t)jx * jy * jz;
+    if ((rc = dalloc(h, (void**)&h->fi_c, 8 * nfi)) || (rc = dalloc(h, (void**)&h->rhs_c, 8 * nrh))) return rc;
+    // Jacobi wall-fill passes from its contraction factor
+    unsigned long long* qd;
+    if ((rc = dalloc(h, (void**)&qd, 8))) return rc;
+    k_wall_contraction<<<dim3((g.nx + 31) / 32, (g.nz + 3) / 4), dim3(32, 4), 0, h->st>>>(g, h->L[0].cd, qd);
+    unsigned long long qb = 0;
+    CK(cudaMemcpyAsync(&qb, qd, 8, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    double q;
+    std::memcpy(&q, &qb, 8);
+    h->wall_q = q;
+    if (q <= 1e-12) h->wall_passes = 2;
+    else if (q >= 0.9) h->wall_passes = 40;
+    else {
+        int p = (int)std::ceil(std::log(1e-10) / std::log(q));
+        h->wall_passes = p < 2 ? 2 : (p > 40 ? 40 : p);
+    }
+    return PLES_MG_OK;
+}
+
+int upload_cs(ples_mg_handle* h, const double* const cs[6], bool device_ptrs) {
+    const Geom& g = h->L[0].g;
+    const size_t n[6] = {(size_t)g.ny * g.nz, (size_t)g.ny * g.nz, (size_t)g.nx * g.nz,
+                         (size_t)g.nx * g.nz, (size_t)g.nx * g.ny, (size_t)g.nx * g.ny};
+    for (int s = 0; s < 6; ++s) {
+        const double* src = cs ? cs[s] : nullptr;
+        if (!src) { h->cs_c[s] = nullptr; continue; }
+        if (s != 2 && s != 3) { h->cs_c[s] = nullptr; continue; }  // periodic x/z: unused
+        // persistent per-handle buffers, allocated on first use
+        if (!h->cs_buf[s]) {
+            void* buf = nullptr;
+            int rc = dalloc(h, &buf, 8 * n[s]);
+            if (rc) return rc;
+            h->cs_buf[s] = (double*)buf;
+        }
+        h->cs_c[s] = h->cs_buf[s];
+        CK(cudaMemcpyAsync(h->cs_c[s], src, 8 * n[s], device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                           h->st));
+    }
+    return PLES_MG_OK;
+}
+
+template <typename F>
+int with_device(ples_mg_handle* h, F f) {
+    if (!h) return PLES_MG_BAD_ARG;
+    cudaError_t e = cudaSetDevice(h->dev);
+    if (e != cudaSuccess) return fail(h, PLES_MG_CUDA_ERROR, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return f();
+}
+
+int solve_any(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles, ples_mg_stats* st) {
+    return h->d.precision == PLES_MG_PREC_MIXED ? solve_core<float>(h, rel_tol, abs_tol, max_cycles, st)
+                                                : solve_core<double>(h, rel_tol, abs_tol, max_cycles, st);
+}
+
+// temporary FP64 scaled coefficients for any level (operator entry points)
+int coef64_for(ples_mg_handle* h, int lev, Coef<double>& c, std::vector<void*>& tmp) {
+    LevelData& L = h->L[lev - 1];
+    if (L.has_cd) { c = L.cd; return PLES_MG_OK; }
+    double* gr[9];
+    int rc = raw_metric(h, lev, gr, tmp);
+    if (rc) return rc;
+    double** f[9] = {&c.a1, &c.b12, &c.b13, &c.a2, &c.b21, &c.b23, &c.a3, &c.b31, &c.b32};
+    for (auto pp : f) {
+        CK(cudaMalloc((void**)pp, 8 * (size_t)L.g.n));
+        tmp.push_back(*pp);
+    }
+    return scale_into(h, lev, gr, c);
+}
+
+int coef32_for(ples_mg_handle* h, int lev, Coef<float>& c, std::vector<void*>& tmp) {
+    LevelData& L = h->L[lev - 1];
+    if (L.has_cf) { c = L.cf; return PLES_MG_OK; }
+    double* gr[9];
+    int rc = raw_metric(h, lev, gr, tmp);
+    if (rc) return rc;
+    float** f[9] = {&c.a1, &c.b12, &c.b13, &c.a2, &c.b21, &c.b23, &c.a3, &c.b31, &c.b32};
+    for (auto pp : f) {
+        CK(cudaMalloc((void**)pp, 4 * (size_t)L.g.n));
+        tmp.push_back(*pp);
+    }
+    return scale_into(h, lev, gr, c);
+}
+
+int tmp_box(ples_mg_handle* h, const Geom& g, size_t es, void** p, std::vector<void*>& tmp) {
+    CK(cudaMalloc(p, es * (size_t)g.n));
+    tmp.push_back(*p);
+    CK(cudaMemsetAsync(*p, 0, es * (size_t)g.n, h->st));
+    return PLES_MG_OK;
+}
+
+dim3 compact_grid(const Geom& g, int ghost) {
+    return ghost ? dim3((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2)
+                 : dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
+}
+
+int put_box(ples_mg_handle* h, const Geom& g, int ghost, const double* host, double* box, std::vector<void*>& tmp) {
+    const size_t n = ghost ? (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) : (size_t)g.nx * g.ny * g.nz;
+    void* c;
+    CK(cudaMalloc(&c, 8 * n));
+    tmp.push_back(c);
+    CK(cudaMemcpyAsync(c, host, 8 * n, cudaMemcpyHostToDevice, h->st));
+    k_compact_to_box<<<compact_grid(g, ghost), dim3(32, 4), 0, h->st>>>(g, ghost, (const double*)c, box);
+    CK(cudaGetLastError());
+    return PLES_MG_OK;
+}
+
+int get_box(ples_mg_handle* h, const Geom& g, int ghost, const double* box, double* host, std::vector<void*>& tmp) {
+    const size_t n = ghost ? (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) : (size_t)g.nx * g.ny * g.nz;
+    void* c;
+    CK(cudaMalloc(&c, 8 * n));
+    tmp.push_back(c);
+    k_box_to_compact<<<compact_grid(g, ghost), dim3(32, 4), 0, h->st>>>(g, ghost, box, (double*)c);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, c, 8 * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return PLES_MG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+extern "C" {
+
+int ples_mg_create(const ples_mg_desc* desc, ples_mg_handle** out) {
+    if (!out) return PLES_MG_BAD_ARG;
+    *out = nullptr;
+    ples_mg_handle* h = new ples_mg_handle();
+    int rc = create_impl(desc, h);
+    if (rc) {
+        static thread_local std::string last;
+        last = h->err;
+        ples_mg_destroy(h);
+        *out = nullptr;
+        fprintf(stderr, "ples_mg_create: %s\n", last.c_str());
+        return rc;
+    }
+    *out = h;
+    return PLES_MG_OK;
+}
+
+void ples_mg_destroy(ples_mg_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->dev);
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (void* p : h->allocs) cudaFree(p);
+    for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+    if (h->h_red) cudaFreeHost(h->h_red);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+}
+
+const char* ples_mg_strerror(int code) {
+    switch (code) {
+        case PLES_MG_OK: return "ok";
+        case PLES_MG_NOT_CONVERGED: return "not converged within max_cycles";
+        case PLES_MG_BAD_ARG: return "bad argument";
+        case PLES_MG_OOM: return "out of device memory";
+        case PLES_MG_DEVICE_TIMEOUT: return "device wait timed out";
+        case PLES_MG_CUDA_ERROR: return "CUDA error";
+        case PLES_MG_DIVERGED: return "diverged (NaN/Inf or residual growth)";
+        case PLES_MG_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* ples_mg_last_error(const ples_mg_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int ples_mg_levels(const ples_mg_handle* h, int* nlevel) {
+    if (!h || !nlevel) return PLES_MG_BAD_ARG;
+    *nlevel = h->nlev;
+    return PLES_MG_OK;
+}
+
+int ples_mg_level_dims(const ples_mg_handle* h, int level, int* nx, int* ny, int* nz) {
+    if (!h || level < 1 || level > h->nlev || !nx || !ny || !nz) return PLES_MG_BAD_ARG;
+    *nx = h->L[level - 1].g.nx;
+    *ny = h->L[level - 1].g.ny;
+    *nz = h->L[level - 1].g.nz;
+    return PLES_MG_OK;
+}
+
+int ples_mg_solve(ples_mg_handle* h, double* fi, const double* rhs, const double* const cs[6], double rel_tol,
+                  double abs_tol_max, int max_cycles, ples_mg_stats* stats) {
+    if (!h || !fi || !rhs || max_cycles < 0) return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        auto t0 = std::chrono::steady_clock::now();
+        ples_mg_stats st{};
+        const Geom& g = h->L[0].g;
+        const size_t nfi = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2), nrh = (size_t)g.nx * g.ny * g.nz;
+        CK(cudaMemcpyAsync(h->fi_c, fi, 8 * nfi, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->rhs_c, rhs, 8 * nrh, cudaMemcpyHostToDevice, h->st));
+        k_compact_to_box<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->fi_c, h->x);
+        k_compact_to_box<<<compact_grid(g, 0), dim3(32, 4), 0, h->st>>>(g, 0, h->rhs_c, h->b);
+        h->launches += 2;
+        CK(cudaGetLastError());
+        int rc = upload_cs(h, cs, false);
+        if (rc) return rc;
+        rc = solve_any(h, rel_tol, abs_tol_max, max_cycles, &st);
+        if (rc != PLES_MG_OK && rc != PLES_MG_NOT_CONVERGED && rc != PLES_MG_DIVERGED) return rc;
+        k_box_to_compact<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->x, h->fi_c);
+        ++h->launches;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(fi, h->fi_c, 8 * nfi, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (stats) *stats = st;
+        return rc;
+    });
+}
+
+int ples_mg_solve_device(ples_mg_handle* h, double* d_fi, const double* d_rhs, const double* const d_cs[6],
+                         double rel_tol, double abs_tol_max, int max_cycles, void* stream, ples_mg_stats* stats) {
+    if (!h || !d_fi || !d_rhs || max_cycles < 0) return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        auto t0 = std::chrono::steady_clock::now();
+        ples_mg_stats st{};
+        // with a caller stream every kernel of this solve runs on it, in order
+        // with the caller's work (and timeable with events on that stream)
+        struct StreamSwap {
+            ples_mg_handle* h;
+            cudaStream_t saved;
+            ~StreamSwap() { h->st = saved; }
+        } swap_back{h, h->st};
+        if (stream) h->st = (cudaStream_t)stream;
+        const Geom& g = h->L[0].g;
+        k_compact_to_box<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, d_fi, h->x);
+        k_compact_to_box<<<compact_grid(g, 0), dim3(32, 4), 0, h->st>>>(g, 0, d_rhs, h->b);
+        h->launches += 2;
+        CK(cudaGetLastError());
+        int rc = upload_cs(h, d_cs, true);
+        if (rc) return rc;
+        rc = solve_any(h, rel_tol, abs_tol_max, max_cycles, &st);
+        if (rc != PLES_MG_OK && rc != PLES_MG_NOT_CONVERGED && rc != PLES_MG_DIVERGED) return rc;
+        k_box_to_compact<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->x, d_fi);
+        ++h->launches;
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(h->st));
+        st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (stats) *stats = st;
+        return rc;
+    });
+}
+
+int ples_mg_get_metric(ples_mg_handle* h, int level, int which, double* out) {
+    if (!h || level < 1 || level > h->nlev || which < 0 || which > 8 || !out)
+        return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        std::vector<void*> tmp;
+        double* gr[9];
+        int rc = raw_metric(h, level, gr, tmp);
+        if (rc) return rc;
+        const Geom& g = h->L[level - 1].g;
+        int i0 = 1, i1 = g.nx, j0 = 1, j1 = g.ny, k0 = 1, k1 = g.nz;
+        if (which < 3) i0 = 0;
+        else if (which < 6) j0 = 0;
+        else k0 = 0;
+        const size_t n = (size_t)(i1 - i0 + 1) * (j1 - j0 + 1) * (k1 - k0 + 1);
+        void* c;
+        cudaError_t e = cudaMalloc(&c, 8 * n);
+        if (e != cudaSuccess) { free_tmp(tmp); return fail(h, PLES_MG_OOM, "scratch: %s", cudaGetErrorString(e)); }
+        tmp.push_back(c);
+        k_box_extract<<<dim3((i1 - i0 + 1 + 31) / 32, (j1 - j0 + 1 + 3) / 4, k1 - k0 + 1), dim3(32, 4), 0, h->st>>>(
+            g, gr[which], i0, i1, j0, j1, k0, (double*)c);
+        e = cudaMemcpyAsync(out, c, 8 * n, cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        free_tmp(tmp);
+        if (e != cudaSuccess) return fail(h, PLES_MG_CUDA_ERROR, "get_metric: %s", cudaGetErrorString(e));
+        return PLES_MG_OK;
+    });
+}
+
+int ples_mg_apply_residual(ples_mg_handle* h, int level, const double* pr, const double* rh, double* out,
+                           int precision) {
+    if (!h || level < 1 || level > h->nlev || !pr || !rh || !out ||
+        (precision != PLES_MG_PREC_FP64 && precision != PLES_MG_PREC_MIXED))
+        return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        std::vector<void*> tmp;
+        const Geom& g = h->L[level - 1].g;
+        double *P, *R, *O;
+        int rc;
+        if ((rc = tmp_box(h, g, 8, (void**)&P, tmp)) || (rc = tmp_box(h, g, 8, (void**)&R, tmp)) ||
+            (rc = tmp_box(h, g, 8, (void**)&O, tmp)) || (rc = put_box(h, g, 1, pr, P, tmp)) ||
+            (rc = put_box(h, g, 0, rh, R, tmp))) {
+            free_tmp(tmp);
+            return rc;
+        }
+        dim3 blk(32, 4), grd((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
+        if (precision == PLES_MG_PREC_FP64) {
+            Coef<double> c;
+            if ((rc = coef64_for(h, level, c, tmp))) { free_tmp(tmp); return rc; }
+            k_residual<double><<<grd, blk, 0, h->st>>>(g, c, P, R, O);
+        } else {
+            Coef<float> c;
+            float *P32, *R32, *O32;
+            if ((rc = coef32_for(h, level, c, tmp)) || (rc = tmp_box(h, g, 4, (void**)&P32, tmp)) ||
+                (rc = tmp_box(h, g, 4, (void**)&R32, tmp)) || (rc = tmp_box(h, g, 4, (void**)&O32, tmp))) {
+                free_tmp(tmp);
+                return rc;
+            }
+            k_convert<float, double><<<grid1(g.n), 256, 0, h->st>>>(g.n, P, P32);
+            k_convert<float, double><<<grid1(g.n), 256, 0, h->st>>>(g.n, R, R32);
+            k_residual<float><<<grd, blk, 0, h->st>>>(g, c, P32, R32, O32);
+            k_convert<double, float><<<grid1(g.n), 256, 0, h->st>>>(g.n, O32, O);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { free_tmp(tmp); return fail(h, PLES_MG_CUDA_ERROR, "residual: %s", cudaGetErrorString(e)); }
+        rc = get_box(h, g, 0, O, out, tmp);
+        free_tmp(tmp);
+        return rc;
+    });
+}
+
+int ples_mg_apply_ghost_fill(ples_mg_handle* h, int level, double* pr, const double* const cs[6], int passes) {
+    if (!h || level < 1 || level > h->nlev || !pr || passes < 1)
+        return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        std::vector<void*> tmp;
+        const Geom& g = h->L[level - 1].g;
+        double* P;
+        Coef<double> c;
+        int rc;
+        if ((rc = tmp_box(h, g, 8, (void**)&P, tmp)) || (rc = put_box(h, g, 1, pr, P, tmp)) ||
+            (rc = coef64_for(h, level, c, tmp))) {
+            free_tmp(tmp);
+            return rc;
+        }
+        const double* c3 = nullptr;
+        const double* c4 = nullptr;
+        if (level == 1 && cs) {
+            if ((rc = upload_cs(h, cs, false))) { free_tmp(tmp); return rc; }
+            c3 = h->cs_c[2];
+            c4 = h->cs_c[3];
+        }
+        // the handle's wall buffer is sized for level 1 and serves every level
+        wall_fill(h, P, c3, c4, level == 1 ? 1.0 / h->d.dt : 0.0, passes, g, c);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { free_tmp(tmp); return fail(h, PLES_MG_CUDA_ERROR, "ghost fill: %s", cudaGetErrorString(e)); }
+        rc = get_box(h, g, 1, P, pr, tmp);
+        free_tmp(tmp);
+        return rc;
+    });
+}
+
+int ples_mg_apply_restrict(ples_mg_handle* h, int level, const double* rh, double* out) {
+    if (!h || level < 1 || level >= h->nlev || !rh || !out)
+        return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        std::vector<void*> tmp;
+        const Geom& gf = h->L[level - 1].g;
+        const Geom& gc = h->L[level].g;
+        double *F, *C;
+        int rc;
+        if ((rc = tmp_box(h, gf, 8, (void**)&F, tmp)) || (rc = tmp_box(h, gc, 8, (void**)&C, tmp)) ||
+            (rc = put_box(h, gf, 0, rh, F, tmp))) {
+            free_tmp(tmp);
+            return rc;
+        }
+        k_restrict<double><<<dim3((gc.nx + 31) / 32, (gc.ny + 3) / 4, gc.nz), dim3(32, 4), 0, h->st>>>(gf, gc, F, C);
+        rc = get_box(h, gc, 0, C, out, tmp);
+        free_tmp(tmp);
+        return rc;
+    });
+}
+
+int ples_mg_apply_prolong(ples_mg_handle* h, int level, double* prf, const double* prc) {
+    if (!h || level < 1 || level >= h->nlev || !prf || !prc)
+        return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        std::vector<void*> tmp;
+        const Geom& gf = h->L[level - 1].g;
+        const Geom& gc = h->L[level].g;
+        double *F, *C;
+        int rc;
+        if ((rc = tmp_box(h, gf, 8, (void**)&F, tmp)) || (rc = tmp_box(h, gc, 8, (void**)&C, tmp)) ||
+            (rc = put_box(h, gf, 1, prf, F, tmp)) || (rc = put_box(h, gc, 1, prc, C, tmp))) {
+            free_tmp(tmp);
+            return rc;
+        }
+        k_prolong<double, double><<<dim3((gc.nx + 1 + 31) / 32, (gc.ny + 1 + 3) / 4, gc.nz + 1), dim3(32, 4), 0,
+                                    h->st>>>(gf, gc, F, C);
+        rc = get_box(h, gf, 1, F, prf, tmp);
+        free_tmp(tmp);
+        return rc;
+    });
+}
+
+int ples_mg_counters(ples_mg_handle* h, long long* launches, long long* device_bytes) {
+    if (!h) return PLES_MG_BAD_ARG;
+    if (launches) *launches = h->launches;
+    if (device_bytes) *device_bytes = h->bytes;
+    return PLES_MG_OK;
+}
+
+int ples_mg_kernel_timing(ples_mg_handle* h, int kind, int level) {
+    if (!h || kind < -1 || kind > 5 || (kind >= 0 && (level < 1 || level > h->nlev))) return PLES_MG_BAD_ARG;
+    h->timed_kind = kind;
+    h->timed_level = level;
+    h->timed_ms = 0.0;
+    h->timed_launches = 0;
+    h->ev_used = 0;
+    return PLES_MG_OK;
+}
+
+int ples_mg_kernel_time(ples_mg_handle* h, double* total_ms, long long* launches) {
+    if (!h) return PLES_MG_BAD_ARG;
+    if (total_ms) *total_ms = h->timed_ms;
+    if (launches) *launches = h->timed_launches;
+    return PLES_MG_OK;
+}
+
+}  // extern "C"

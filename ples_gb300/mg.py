@@ -1,0 +1,267 @@
+"""Host-side interface of the GB300 pressure multigrid, over the C ABI.
+
+`Multigrid` mirrors the reference's set-up/solve split: construction plays
+the part of metrica -> mul_met -> wall (fsrc/stratiParticle.f03:767-769) and
+`multi(eps, ficycle, fi, rhs)` keeps the meaning of the Fortran subroutine
+`multi` (fsrc/multigrid.f03:42-653): an absolute max-norm stop `eps`, at most
+`ficycle` cycles, `fi` updated in place including its ghost layer.  `solve`
+adds the relative L2 stop used by the benchmarks.
+
+Everything runs in libples_mg.so on the GPU; if the library cannot be built
+or loaded, or no GPU is present, construction raises -- there is no CPU path.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK, NOT_CONVERGED, BAD_ARG, OOM, DEVICE_TIMEOUT, CUDA_ERROR, DIVERGED, NO_DEVICE = range(8)
+PREC_FP64, PREC_MIXED = 0, 1
+COORDS_NODES, COORDS_GHOSTED8 = 0, 1
+METRIC_NAMES = ("g11", "g12", "g13", "g21", "g22", "g23", "g31", "g32", "g33")
+
+
+class PlesMGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Desc(C.Structure):
+    _fields_ = [("jx", C.c_int), ("jy", C.c_int), ("jz", C.c_int),
+                ("ip", C.c_int), ("jp", C.c_int), ("kp", C.c_int),
+                ("nlevmax", C.c_int), ("omega", C.c_double), ("precision", C.c_int),
+                ("coords_layout", C.c_int),
+                ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("z", C.POINTER(C.c_double)), ("dt", C.c_double), ("device", C.c_int),
+                ("nu_pre", C.c_int), ("nu_post", C.c_int), ("nu_coarse", C.c_int),
+                ("inner_cycles", C.c_int), ("smoother", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("outer_iterations", C.c_int), ("vcycles", C.c_int),
+                ("rel_residual", C.c_double), ("max_residual", C.c_double),
+                ("rhs_norm", C.c_double), ("rhs_mean_removed", C.c_double),
+                ("seconds", C.c_double), ("status", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
+
+EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_destroy",
+           "ples_mg_strerror", "ples_mg_last_error", "ples_mg_levels", "ples_mg_level_dims",
+           "ples_mg_get_metric", "ples_mg_apply_residual", "ples_mg_apply_ghost_fill",
+           "ples_mg_apply_restrict", "ples_mg_apply_prolong", "ples_mg_counters",
+           "ples_mg_kernel_timing", "ples_mg_kernel_time")
+KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
+
+
+def load(build=True):
+    """Load libples_mg.so (building it first if its sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise ImportError(f"libples_mg.so not found at {path}; run ples_gb300/build.py")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.ples_mg_create.argtypes = [C.POINTER(Desc), C.POINTER(vp)]
+    L.ples_mg_solve.argtypes = [vp, _dp, _dp, vp, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]
+    L.ples_mg_solve_device.argtypes = [vp, vp, vp, vp, C.c_double, C.c_double, C.c_int, vp,
+                                       C.POINTER(Stats)]
+    L.ples_mg_destroy.argtypes = [vp]
+    L.ples_mg_destroy.restype = None
+    L.ples_mg_strerror.restype = C.c_char_p
+    L.ples_mg_strerror.argtypes = [C.c_int]
+    L.ples_mg_last_error.restype = C.c_char_p
+    L.ples_mg_last_error.argtypes = [vp]
+    L.ples_mg_levels.argtypes = [vp, C.POINTER(C.c_int)]
+    L.ples_mg_level_dims.argtypes = [vp, C.c_int] + [C.POINTER(C.c_int)] * 3
+    L.ples_mg_get_metric.argtypes = [vp, C.c_int, C.c_int, _dp]
+    L.ples_mg_apply_residual.argtypes = [vp, C.c_int, _dp, _dp, _dp, C.c_int]
+    L.ples_mg_apply_ghost_fill.argtypes = [vp, C.c_int, _dp, vp, C.c_int]
+    L.ples_mg_apply_restrict.argtypes = [vp, C.c_int, _dp, _dp]
+    L.ples_mg_apply_prolong.argtypes = [vp, C.c_int, _dp, _dp]
+    L.ples_mg_counters.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.ples_mg_kernel_timing.argtypes = [vp, C.c_int, C.c_int]
+    L.ples_mg_kernel_time.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    _lib = L
+    return L
+
+
+def _f64(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def _cs_ptrs(cs):
+    if cs is None:
+        return None, None
+    keep = [None if a is None else _f64(a) for a in cs]
+    arr = (C.c_void_p * 6)(*[None if a is None else a.ctypes.data for a in keep])
+    return C.cast(arr, C.c_void_p), (keep, arr)
+
+
+class Multigrid:
+    """One grid's coefficient hierarchy, resident on the GPU."""
+
+    def __init__(self, x, y, z, ip=0, jp=1, kp=0, precision="mixed", dt=1.0, device=0,
+                 nlevmax=0, omega=0.0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0,
+                 smoother=0, coords_layout=COORDS_NODES, jx=None, jy=None, jz=None):
+        self._L = load()
+        self._x, self._y, self._z = _f64(x), _f64(y), _f64(z)
+        if coords_layout == COORDS_NODES:
+            jx, jy, jz = (s - 1 for s in self._x.shape)
+        else:
+            jx, jy, jz = (s - 17 for s in self._x.shape)
+        self.jx, self.jy, self.jz = jx, jy, jz
+        self.precision = {"mixed": PREC_MIXED, "fp64": PREC_FP64}.get(precision, precision)
+        d = Desc()
+        d.jx, d.jy, d.jz, d.ip, d.jp, d.kp = jx, jy, jz, ip, jp, kp
+        d.nlevmax, d.omega, d.precision, d.coords_layout = nlevmax, omega, self.precision, coords_layout
+        dp = C.POINTER(C.c_double)
+        d.x = self._x.ctypes.data_as(dp)
+        d.y = self._y.ctypes.data_as(dp)
+        d.z = self._z.ctypes.data_as(dp)
+        d.dt, d.device = dt, device
+        d.nu_pre, d.nu_post, d.nu_coarse = nu_pre, nu_post, nu_coarse
+        d.inner_cycles, d.smoother = inner_cycles, smoother
+        h = C.c_void_p()
+        rc = self._L.ples_mg_create(C.byref(d), C.byref(h))
+        if rc != OK:
+            raise PlesMGError(rc, self._L.ples_mg_strerror(rc).decode())
+        self._h = h
+
+    # -- lifetime --------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ples_mg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, allow=(OK,)):
+        if rc not in allow:
+            msg = self._L.ples_mg_last_error(self._h).decode() if self._h else ""
+            raise PlesMGError(rc, f"{self._L.ples_mg_strerror(rc).decode()}: {msg}")
+        return rc
+
+    # -- levels ------------------------------------------------------------
+    @property
+    def nlevel(self):
+        n = C.c_int()
+        self._check(self._L.ples_mg_levels(self._h, C.byref(n)))
+        return n.value
+
+    def dims(self, level):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        self._check(self._L.ples_mg_level_dims(self._h, level, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    # -- solves --------------------------------------------------------------
+    def solve(self, rhs, fi=None, cs=None, rel_tol=1e-10, abs_tol=0.0, max_cycles=200):
+        """Returns (fi, stats dict); fi (jx+2, jy+2, jz+2) with ghosts."""
+        if fi is None:
+            fi = np.zeros((self.jx + 2, self.jy + 2, self.jz + 2), order="F")
+        else:
+            fi = _f64(fi).copy(order="F")
+        st = Stats()
+        ptr, keep = _cs_ptrs(cs)
+        rc = self._L.ples_mg_solve(self._h, fi, _f64(rhs), ptr, rel_tol, abs_tol, max_cycles,
+                                   C.byref(st))
+        self._check(rc, allow=(OK, NOT_CONVERGED))
+        return fi, st.as_dict()
+
+    def multi(self, eps, ficycle, fi, rhs, cs=None):
+        """The reference's entry point: fi updated in place, stop on
+        max|r| < eps or ficycle cycles; returns the cycle count."""
+        if not (isinstance(fi, np.ndarray) and fi.dtype == np.float64 and fi.flags.f_contiguous):
+            raise TypeError("fi must be a Fortran-ordered float64 array (0:jx+1,0:jy+1,0:jz+1)")
+        st = Stats()
+        ptr, keep = _cs_ptrs(cs)
+        rc = self._L.ples_mg_solve(self._h, fi, _f64(rhs), ptr, 0.0, eps, ficycle, C.byref(st))
+        self._check(rc, allow=(OK, NOT_CONVERGED))
+        return st.outer_iterations
+
+    def solve_device(self, d_fi, d_rhs, rel_tol=1e-10, abs_tol=0.0, max_cycles=200, stream=0,
+                     d_cs=None):
+        """Device-resident solve; d_fi/d_rhs are CUDA buffers (integer device
+        pointers, e.g. torch_tensor.data_ptr()) in Fortran layout."""
+        st = Stats()
+        ptr = None
+        if d_cs is not None:
+            arr = (C.c_void_p * 6)(*[None if p is None else int(p) for p in d_cs])
+            ptr = C.cast(arr, C.c_void_p)
+        rc = self._L.ples_mg_solve_device(self._h, C.c_void_p(int(d_fi)), C.c_void_p(int(d_rhs)), ptr,
+                                          rel_tol, abs_tol, max_cycles, C.c_void_p(int(stream)),
+                                          C.byref(st))
+        self._check(rc, allow=(OK, NOT_CONVERGED))
+        return st.as_dict()
+
+    # -- instrumentation ------------------------------------------------------
+    def counters(self):
+        n, b = C.c_longlong(), C.c_longlong()
+        self._check(self._L.ples_mg_counters(self._h, C.byref(n), C.byref(b)))
+        return {"launches": n.value, "device_bytes": b.value}
+
+    def time_kernel(self, kind, level=1):
+        """Start CUDA-event timing of one kernel kind ('line', 'restrict',
+        'prolong', 'outer' or None to stop) at one level."""
+        k = -1 if kind is None else KERNEL_KINDS[kind]
+        self._check(self._L.ples_mg_kernel_timing(self._h, k, level))
+
+    def kernel_time(self):
+        ms, n = C.c_double(), C.c_longlong()
+        self._check(self._L.ples_mg_kernel_time(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    # -- per-level operators -------------------------------------------------
+    def metric(self, level, which):
+        w = METRIC_NAMES.index(which)
+        nx, ny, nz = self.dims(level)
+        shape = [(nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1)][w // 3]
+        out = np.zeros(shape, order="F")
+        self._check(self._L.ples_mg_get_metric(self._h, level, w, out))
+        return out
+
+    def residual(self, level, pr, rh, precision="fp64"):
+        nx, ny, nz = self.dims(level)
+        out = np.zeros((nx, ny, nz), order="F")
+        p = {"fp64": PREC_FP64, "fp32": PREC_MIXED, "mixed": PREC_MIXED}[precision]
+        self._check(self._L.ples_mg_apply_residual(self._h, level, _f64(pr), _f64(rh), out, p))
+        return out
+
+    def ghost_fill(self, level, pr, cs=None, passes=30):
+        pr = _f64(pr).copy(order="F")
+        ptr, keep = _cs_ptrs(cs)
+        self._check(self._L.ples_mg_apply_ghost_fill(self._h, level, pr, ptr, passes))
+        return pr
+
+    def restrict(self, level, rh):
+        nx, ny, nz = self.dims(level + 1)
+        out = np.zeros((nx, ny, nz), order="F")
+        self._check(self._L.ples_mg_apply_restrict(self._h, level, _f64(rh), out))
+        return out
+
+    def prolong(self, level, prf, prc):
+        prf = _f64(prf).copy(order="F")
+        self._check(self._L.ples_mg_apply_prolong(self._h, level, prf, _f64(prc)))
+        return prf

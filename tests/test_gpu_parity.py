@@ -1,0 +1,223 @@
+"""Parity of the CUDA path with the CPU oracle, through the C ABI.
+
+Tolerances:
+* face metric: bit-exact (same FP64 expressions, no FMA contraction);
+* FP64 residual: max |dev - oracle| <= 1e-12 * max |oracle| (summation order
+  differs); FP32 residual: <= 2e-5 relative to the largest flux term;
+* ghost layer at the fixed point of the fill: <= 1e-12 relative;
+* restriction bit-exact, prolongation <= 1e-14;
+* solves converged to ||r||/||b|| <= 1e-10: zero-mean solution within 1e-8
+  of the oracle's converged solution in the L2 and max norms, and the
+  device solution satisfies the oracle's discrete system (its own FP64
+  residual of the device solution) to <= 2e-10.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from ples_gb300 import mg
+from ples_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-10
+SOL_TOL = 1e-8
+
+
+def _zm(fi):
+    p = fi[1:-1, 1:-1, 1:-1]
+    return p - p.mean()
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b), np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.fixture(scope="module")
+def case0():
+    w = S.WORKLOADS["channel_64x32x64"]
+    x, y, z = w.grid()
+    rhs = w.rhs()
+    orc = Oracle(x, y, z, islor=1)
+    fi, cyc, rm, rr = orc.multi(rhs, eps=1e-13, ficycle=300)
+    assert rr <= 1e-13
+    return dict(x=x, y=y, z=z, rhs=rhs, orc=orc, ref=_zm(fi))
+
+
+@pytest.fixture(scope="module")
+def dev_mixed(case0):
+    with mg.Multigrid(case0["x"], case0["y"], case0["z"], precision="mixed") as m:
+        yield m
+
+
+@pytest.fixture(scope="module")
+def dev_fp64(case0):
+    with mg.Multigrid(case0["x"], case0["y"], case0["z"], precision="fp64") as m:
+        yield m
+
+
+@pytest.mark.parametrize("level", [1, 2, 3, 4])
+def test_metric_bit_exact(case0, dev_mixed, level):
+    for name in mg.METRIC_NAMES:
+        a = dev_mixed.metric(level, name)
+        b = case0["orc"].metric(level, name)
+        assert a.shape == b.shape
+        assert np.array_equal(a, b), (name, np.abs(a - b).max())
+
+
+def test_metric_sample_deck_and_ghosted_layout():
+    import json, os
+    d = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "sample_deck.json")))
+    xs, ys, zs = (np.array(d[c]) for c in "xyz")
+    shp = (xs.size, ys.size, zs.size)
+    x = np.asfortranarray(np.broadcast_to(xs[:, None, None], shp))
+    y = np.asfortranarray(np.broadcast_to(ys[None, :, None], shp))
+    z = np.asfortranarray(np.broadcast_to(zs[None, None, :], shp))
+    orc = Oracle(x, y, z)
+    # the ghosted (-8:n+8) layout as PLES holds it after cellep
+    gx, gy, gz = (orc.coords(c) for c in range(3))
+    with mg.Multigrid(gx, gy, gz, coords_layout=mg.COORDS_GHOSTED8) as m:
+        assert (m.jx, m.jy, m.jz) == (32, 32, 32)
+        for level in (1, 2, 3, 4):
+            for name in mg.METRIC_NAMES:
+                assert np.array_equal(m.metric(level, name), orc.metric(level, name)), (level, name)
+
+
+@pytest.mark.parametrize("level", [1, 2, 3])
+def test_residual_fp64_and_fp32(case0, dev_mixed, level):
+    orc = case0["orc"]
+    nx, ny, nz = orc.dims(level)
+    rng = np.random.default_rng(level)
+    pr = np.asfortranarray(rng.standard_normal((nx + 2, ny + 2, nz + 2)))
+    rh = np.asfortranarray(rng.standard_normal((nx, ny, nz)))
+    ref = orc.resid(level, pr, rh)
+    r64 = dev_mixed.residual(level, pr, rh, "fp64")
+    assert np.abs(r64 - ref).max() <= 1e-12 * np.abs(ref).max()
+    r32 = dev_mixed.residual(level, pr, rh, "fp32")
+    scale = np.abs(orc.resid(level, pr, np.zeros_like(rh))).max() + np.abs(rh).max()
+    assert np.abs(r32 - ref).max() <= 2e-5 * scale
+
+
+@pytest.mark.parametrize("level", [1, 2])
+def test_ghost_fill_fixed_point(case0, dev_mixed, level):
+    orc = case0["orc"]
+    nx, ny, nz = orc.dims(level)
+    rng = np.random.default_rng(10 + level)
+    pr = np.asfortranarray(rng.standard_normal((nx + 2, ny + 2, nz + 2)))
+    # cs1,cs2 (1:jy,1:jz), cs3,cs4 (1:jx,1:jz), cs5,cs6 (1:jx,1:jy) of the fine grid
+    shapes = ((32, 64), (32, 64), (64, 64), (64, 64), (64, 32), (64, 32))
+    cs = [np.asfortranarray(rng.standard_normal(s)) for s in shapes]
+    ref = pr.copy(order="F")
+    for _ in range(12):
+        ref = orc.ghost_fill(level, ref, cs=cs)
+    out = dev_mixed.ghost_fill(level, pr, cs=cs, passes=60)
+    np.testing.assert_array_equal(out[1:-1, 1:-1, 1:-1], pr[1:-1, 1:-1, 1:-1])
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_restriction_and_prolongation(case0, dev_mixed):
+    orc = case0["orc"]
+    rng = np.random.default_rng(4)
+    for level in (1, 2, 3):
+        nx, ny, nz = orc.dims(level)
+        r = np.asfortranarray(rng.standard_normal((nx, ny, nz)))
+        assert np.array_equal(dev_mixed.restrict(level, r), orc.restrict(level, r))
+        cx, cy, cz = orc.dims(level + 1)
+        pf = np.asfortranarray(rng.standard_normal((nx + 2, ny + 2, nz + 2)))
+        pc = np.asfortranarray(rng.standard_normal((cx + 2, cy + 2, cz + 2)))
+        a = dev_mixed.prolong(level, pf, pc)
+        b = orc.prolong(level, pf, pc)
+        assert np.abs(a - b).max() <= 1e-14 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_solve_parity(case0, dev_mixed, dev_fp64, prec):
+    m = dev_mixed if prec == "mixed" else dev_fp64
+    fi, st = m.solve(case0["rhs"], rel_tol=REL_TOL, max_cycles=100)
+    assert st["status"] == mg.OK and st["rel_residual"] <= REL_TOL
+    l2, mx = _rel(_zm(fi), case0["ref"])
+    assert l2 <= SOL_TOL and mx <= SOL_TOL, (l2, mx)
+    r, _ = case0["orc"].true_residual(fi, case0["rhs"])
+    assert np.linalg.norm(r) / np.linalg.norm(case0["rhs"]) <= 2e-10
+    # warm start from the solution: already converged
+    fi2, st2 = m.solve(case0["rhs"], fi=fi, rel_tol=REL_TOL)
+    assert st2["outer_iterations"] == 0
+
+
+def test_solve_with_wall_fluxes_and_dt():
+    """cs3/cs4 (wall flux mismatches, contra.f03) with dt != 1: the device
+    solution matches the oracle's converged solution."""
+    jx, jy, jz, dt = 32, 16, 32, 0.5
+    x, y, z = S.wavy_channel_grid(jx, jy, jz, 0.08, 2.0)
+    rng = np.random.default_rng(21)
+    cs3 = np.asfortranarray(0.1 * rng.standard_normal((jx, jz)))
+    cs4 = np.asfortranarray(0.1 * rng.standard_normal((jx, jz)))
+    cs = [np.zeros((jy, jz), order="F"), np.zeros((jy, jz), order="F"), cs3, cs4,
+          np.zeros((jx, jy), order="F"), np.zeros((jx, jy), order="F")]
+    rhs = S.divergence_rhs(jx, jy, jz, 5, dt)
+    rhs = rhs + (cs4.sum() - cs3.sum()) / dt / rhs.size  # compatible with the wall fluxes
+    orc = Oracle(x, y, z, islor=1, dt=dt)
+    fo, cyc, rm, rr = orc.multi(rhs, cs=cs, eps=1e-13, ficycle=300)
+    with mg.Multigrid(x, y, z, dt=dt) as m:
+        fi, st = m.solve(rhs, cs=cs, rel_tol=REL_TOL)
+        assert st["status"] == mg.OK
+        assert abs(st["rhs_mean_removed"]) < 1e-12
+    l2, mx = _rel(_zm(fi), _zm(fo))
+    assert l2 <= SOL_TOL and mx <= SOL_TOL, (l2, mx)
+    r, _ = orc.true_residual(fi, rhs, cs=cs)
+    assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 2e-10
+
+
+def test_multi_reference_semantics(case0, dev_mixed):
+    """multi(eps, ficycle, fi, rhs): absolute max-norm stop, fi in place."""
+    fi = np.zeros((66, 34, 66), order="F")
+    cycles = dev_mixed.multi(1e-8, 1000, fi, case0["rhs"])
+    assert cycles > 0
+    r, _ = case0["orc"].true_residual(fi, case0["rhs"])
+    assert np.abs(r).max() < 1.5e-8
+    # the cap on cycles is honoured and reported as not converged
+    fi2 = np.zeros((66, 34, 66), order="F")
+    _, st = dev_mixed.solve(case0["rhs"], fi=fi2, rel_tol=1e-14, max_cycles=2)
+    assert st["status"] == mg.NOT_CONVERGED and st["outer_iterations"] == 2
+
+
+def test_zebra_smoother_same_solution(case0):
+    with mg.Multigrid(case0["x"], case0["y"], case0["z"], smoother=1) as m:
+        fi, st = m.solve(case0["rhs"], rel_tol=REL_TOL)
+    assert st["status"] == mg.OK
+    l2, mx = _rel(_zm(fi), case0["ref"])
+    assert l2 <= SOL_TOL and mx <= SOL_TOL
+
+
+def test_odd_level_counts_and_small_grids():
+    for dims in ((48, 32, 48), (16, 8, 16), (32, 64, 32)):
+        x, y, z = S.wavy_channel_grid(*dims, 0.05, 1.5)
+        rhs = S.divergence_rhs(*dims, seed=3)
+        orc = Oracle(x, y, z, islor=1)
+        fo, *_ = orc.multi(rhs, eps=1e-13, ficycle=400)
+        with mg.Multigrid(x, y, z) as m:
+            fi, st = m.solve(rhs, rel_tol=REL_TOL)
+        assert st["status"] == mg.OK, (dims, st)
+        l2, mx = _rel(_zm(fi), _zm(fo))
+        assert l2 <= SOL_TOL and mx <= SOL_TOL, (dims, l2, mx)
+
+
+def test_full_size_solution_satisfies_reference_system():
+    """256x128x256 (the benchmark grid): the oracle is too slow to solve it
+    here, so check size-independent properties: the device solution is a
+    solution of the oracle's discrete system (FP64 residual of the
+    restatement), and the mixed and FP64 device solutions agree."""
+    w = S.WORKLOADS["channel_256x128x256"]
+    x, y, z = w.grid()
+    rhs = w.rhs()
+    with mg.Multigrid(x, y, z, precision="mixed") as m:
+        fm, sm = m.solve(rhs, rel_tol=REL_TOL)
+    assert sm["status"] == mg.OK
+    orc = Oracle(x, y, z, islor=1)
+    r, _ = orc.true_residual(fm, rhs, passes=6)
+    assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 2e-10
+    with mg.Multigrid(x, y, z, precision="fp64") as m:
+        fd, sd = m.solve(rhs, rel_tol=REL_TOL)
+    assert sd["status"] == mg.OK
+    l2, mx = _rel(_zm(fm), _zm(fd))
+    assert l2 <= SOL_TOL and mx <= SOL_TOL, (l2, mx)
