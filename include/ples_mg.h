@@ -61,7 +61,10 @@ typedef struct {
     int nu_pre, nu_post;   /* smoothing sweeps per level (0 = default)              */
     int nu_coarse;         /* sweeps on the coarsest level (0 = default)            */
     int inner_cycles;      /* V-cycles per outer FP64 iteration (0 = default)       */
-    int smoother;          /* 0 = eta-line Jacobi, 1 = 4-colour zebra eta-line SOR  */
+    int smoother;          /* 0 = zebra eta-line SOR (Gauss-Seidel in x and z as the
+                              reference's line SOR), 1 = eta-line Jacobi         */
+    int coarsening;        /* 0 = full, the reference's hierarchy (mul_met);
+                              1 = semi-coarsening where x/z spacings differ     */
 } ples_mg_desc;
 
 typedef struct {

@@ -1,9 +1,12 @@
 // metric.cu -- face metric of every multigrid level, computed on the device
 // in FP64 from the fine node coordinates.
 //
-// Level n uses the fine nodes sub-sampled with stride s = 2^(n-1):
-//   s == 1 : metrica, fsrc/metrica.f03:85-419
-//   s  > 1 : mul_met, fsrc/multigrid.f03:2520-2988, divided by pot = s,
+// A level uses the fine nodes sub-sampled with strides (sx,sy,sz):
+//   all 1                 : metrica, fsrc/metrica.f03:85-419
+//   sx = sy = sz = 2^(n-1): mul_met, fsrc/multigrid.f03:2520-2988, divided
+//                           by pot = 2^(n-1) (inv_div = 1/pot)
+//   other strides         : the same formulas along each direction with its
+//                           own stride (semi-coarsened levels),
 // with the contravariant rows of gprima/gseconda/gterza.f03.  Ghost nodes
 // outside [0,jx] x [0,jz] follow cellep.f03:29-99 (periodic shift by the
 // domain length along x and z), evaluated on the fly, so any stride whose
@@ -90,15 +93,16 @@ __device__ void metric_row(int row, double xcsi, double ycsi, double zcsi, doubl
 #define AVG_K(F, a1, a2, b1, b2, c) (.25 * (N.F(a2, b2, c) + N.F(a2, b1, c) + N.F(a1, b1, c) + N.F(a1, b2, c)))
 
 // csi faces i = 0..nx (multigrid.f03:2520-2666 / metrica.f03:85-197)
-__global__ void k_metric_csi(Nodes N, Geom g, int s, double inv_pot, double* g11, double* g12, double* g13) {
+__global__ void k_metric_csi(Nodes N, Geom g, int sx, int sy, int sz, double inv_pot, double* g11, double* g12,
+                             double* g13) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
-    const int j2 = j * s, j1 = (j - 1) * s, k2 = k * s, k1 = (k - 1) * s, ic = i * s;
+    const int j2 = j * sy, j1 = (j - 1) * sy, k2 = k * sz, k1 = (k - 1) * sz, ic = i * sx;
     double xcsi, ycsi, zcsi;
     if (i == 0 && N.ip == 1) {
-        const int i1 = s, i2 = 2 * s;
+        const int i1 = sx, i2 = 2 * sx;
         double x2 = AVG_I(X, i2, j1, j2, k1, k2), x1 = AVG_I(X, i1, j1, j2, k1, k2), x0 = AVG_I(X, 0, j1, j2, k1, k2);
         double y2 = AVG_I(Y, i2, j1, j2, k1, k2), y1 = AVG_I(Y, i1, j1, j2, k1, k2), y0 = AVG_I(Y, 0, j1, j2, k1, k2);
         double z2 = AVG_I(Z, i2, j1, j2, k1, k2), z1 = AVG_I(Z, i1, j1, j2, k1, k2), z0 = AVG_I(Z, 0, j1, j2, k1, k2);
@@ -106,7 +110,7 @@ __global__ void k_metric_csi(Nodes N, Geom g, int s, double inv_pot, double* g11
         ycsi = .5 * (-3. * y0 + 4. * y1 - y2);
         zcsi = .5 * (-3. * z0 + 4. * z1 - z2);
     } else if (i == g.nx && N.ip == 1) {
-        const int i1 = (i - 1) * s, i2 = (i - 2) * s, ie = N.jx;
+        const int i1 = (i - 1) * sx, i2 = (i - 2) * sx, ie = N.jx;
         double x2 = AVG_I(X, i2, j1, j2, k1, k2), x1 = AVG_I(X, i1, j1, j2, k1, k2), x0 = AVG_I(X, ie, j1, j2, k1, k2);
         double y2 = AVG_I(Y, i2, j1, j2, k1, k2), y1 = AVG_I(Y, i1, j1, j2, k1, k2), y0 = AVG_I(Y, ie, j1, j2, k1, k2);
         double z2 = AVG_I(Z, i2, j1, j2, k1, k2), z1 = AVG_I(Z, i1, j1, j2, k1, k2), z0 = AVG_I(Z, ie, j1, j2, k1, k2);
@@ -114,7 +118,7 @@ __global__ void k_metric_csi(Nodes N, Geom g, int s, double inv_pot, double* g11
         ycsi = .5 * (3. * y0 - 4. * y1 + y2);
         zcsi = .5 * (3. * z0 - 4. * z1 + z2);
     } else {
-        const int i2 = (i + 1) * s, i1 = (i - 1) * s;
+        const int i2 = (i + 1) * sx, i1 = (i - 1) * sx;
         double xdx = AVG_I(X, i2, j1, j2, k1, k2), xsn = AVG_I(X, i1, j1, j2, k1, k2);
         double ydx = AVG_I(Y, i2, j1, j2, k1, k2), ysn = AVG_I(Y, i1, j1, j2, k1, k2);
         double zdx = AVG_I(Z, i2, j1, j2, k1, k2), zsn = AVG_I(Z, i1, j1, j2, k1, k2);
@@ -131,7 +135,7 @@ __global__ void k_metric_csi(Nodes N, Geom g, int s, double inv_pot, double* g11
     double t[3];
     metric_row(0, xcsi, ycsi, zcsi, xeta, yeta, zeta, xzet, yzet, zzet, t);
     const long long q = g.at(i, j, k);
-    if (s == 1) {
+    if (sx == 1 && sy == 1 && sz == 1) {
         g11[q] = t[0]; g12[q] = t[1]; g13[q] = t[2];
     } else {
         g11[q] = t[0] * inv_pot; g12[q] = t[1] * inv_pot; g13[q] = t[2] * inv_pot;
@@ -139,15 +143,16 @@ __global__ void k_metric_csi(Nodes N, Geom g, int s, double inv_pot, double* g11
 }
 
 // eta faces j = 0..ny (multigrid.f03:2675-2827 / metrica.f03:203-294)
-__global__ void k_metric_eta(Nodes N, Geom g, int s, double inv_pot, double* g21, double* g22, double* g23) {
+__global__ void k_metric_eta(Nodes N, Geom g, int sx, int sy, int sz, double inv_pot, double* g21, double* g22,
+                             double* g23) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
-    const int i2 = i * s, i1 = (i - 1) * s, k2 = k * s, k1 = (k - 1) * s, jc = j * s;
+    const int i2 = i * sx, i1 = (i - 1) * sx, k2 = k * sz, k1 = (k - 1) * sz, jc = j * sy;
     double xeta, yeta, zeta;
     if (j == 0 && N.jp == 1) {
-        const int j1 = s, j2 = 2 * s;
+        const int j1 = sy, j2 = 2 * sy;
         double x2 = AVG_J(X, i1, i2, j2, k1, k2), x1 = AVG_J(X, i1, i2, j1, k1, k2), x0 = AVG_J(X, i1, i2, 0, k1, k2);
         double y2 = AVG_J(Y, i1, i2, j2, k1, k2), y1 = AVG_J(Y, i1, i2, j1, k1, k2), y0 = AVG_J(Y, i1, i2, 0, k1, k2);
         double z2 = AVG_J(Z, i1, i2, j2, k1, k2), z1 = AVG_J(Z, i1, i2, j1, k1, k2), z0 = AVG_J(Z, i1, i2, 0, k1, k2);
@@ -155,7 +160,7 @@ __global__ void k_metric_eta(Nodes N, Geom g, int s, double inv_pot, double* g21
         yeta = .5 * (-3. * y0 + 4. * y1 - y2);
         zeta = .5 * (-3. * z0 + 4. * z1 - z2);
     } else if (j == g.ny && N.jp == 1) {
-        const int j1 = (j - 1) * s, j2 = (j - 2) * s, je = N.jy;
+        const int j1 = (j - 1) * sy, j2 = (j - 2) * sy, je = N.jy;
         double x2 = AVG_J(X, i1, i2, j2, k1, k2), x1 = AVG_J(X, i1, i2, j1, k1, k2), x0 = AVG_J(X, i1, i2, je, k1, k2);
         double y2 = AVG_J(Y, i1, i2, j2, k1, k2), y1 = AVG_J(Y, i1, i2, j1, k1, k2), y0 = AVG_J(Y, i1, i2, je, k1, k2);
         double z2 = AVG_J(Z, i1, i2, j2, k1, k2), z1 = AVG_J(Z, i1, i2, j1, k1, k2), z0 = AVG_J(Z, i1, i2, je, k1, k2);
@@ -163,7 +168,7 @@ __global__ void k_metric_eta(Nodes N, Geom g, int s, double inv_pot, double* g21
         yeta = .5 * (3. * y0 - 4. * y1 + y2);
         zeta = .5 * (3. * z0 - 4. * z1 + z2);
     } else {
-        const int j2 = (j + 1) * s, j1 = (j - 1) * s;
+        const int j2 = (j + 1) * sy, j1 = (j - 1) * sy;
         double xsop = AVG_J(X, i1, i2, j2, k1, k2), xsot = AVG_J(X, i1, i2, j1, k1, k2);
         double ysop = AVG_J(Y, i1, i2, j2, k1, k2), ysot = AVG_J(Y, i1, i2, j1, k1, k2);
         double zsop = AVG_J(Z, i1, i2, j2, k1, k2), zsot = AVG_J(Z, i1, i2, j1, k1, k2);
@@ -180,7 +185,7 @@ __global__ void k_metric_eta(Nodes N, Geom g, int s, double inv_pot, double* g21
     double t[3];
     metric_row(1, xcsi, ycsi, zcsi, xeta, yeta, zeta, xzet, yzet, zzet, t);
     const long long q = g.at(i, j, k);
-    if (s == 1) {
+    if (sx == 1 && sy == 1 && sz == 1) {
         g21[q] = t[0]; g22[q] = t[1]; g23[q] = t[2];
     } else {
         g21[q] = t[0] * inv_pot; g22[q] = t[1] * inv_pot; g23[q] = t[2] * inv_pot;
@@ -188,15 +193,16 @@ __global__ void k_metric_eta(Nodes N, Geom g, int s, double inv_pot, double* g21
 }
 
 // zeta faces k = 0..nz (multigrid.f03:2836-2988 / metrica.f03:316-419)
-__global__ void k_metric_zet(Nodes N, Geom g, int s, double inv_pot, double* g31, double* g32, double* g33) {
+__global__ void k_metric_zet(Nodes N, Geom g, int sx, int sy, int sz, double inv_pot, double* g31, double* g32,
+                             double* g33) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z;
     if (i > g.nx || j > g.ny) return;
-    const int i2 = i * s, i1 = (i - 1) * s, j2 = j * s, j1 = (j - 1) * s, kc = k * s;
+    const int i2 = i * sx, i1 = (i - 1) * sx, j2 = j * sy, j1 = (j - 1) * sy, kc = k * sz;
     double xzet, yzet, zzet;
     if (k == 0 && N.kp == 1) {
-        const int k1 = s, k2 = 2 * s;
+        const int k1 = sz, k2 = 2 * sz;
         double x2 = AVG_K(X, i1, i2, j1, j2, k2), x1 = AVG_K(X, i1, i2, j1, j2, k1), x0 = AVG_K(X, i1, i2, j1, j2, 0);
         double y2 = AVG_K(Y, i1, i2, j1, j2, k2), y1 = AVG_K(Y, i1, i2, j1, j2, k1), y0 = AVG_K(Y, i1, i2, j1, j2, 0);
         double z2 = AVG_K(Z, i1, i2, j1, j2, k2), z1 = AVG_K(Z, i1, i2, j1, j2, k1), z0 = AVG_K(Z, i1, i2, j1, j2, 0);
@@ -204,7 +210,7 @@ __global__ void k_metric_zet(Nodes N, Geom g, int s, double inv_pot, double* g31
         yzet = .5 * (-3. * y0 + 4. * y1 - y2);
         zzet = .5 * (-3. * z0 + 4. * z1 - z2);
     } else if (k == g.nz && N.kp == 1) {
-        const int k1 = (k - 1) * s, k2 = (k - 2) * s, ke = N.jz;
+        const int k1 = (k - 1) * sz, k2 = (k - 2) * sz, ke = N.jz;
         double x2 = AVG_K(X, i1, i2, j1, j2, k2), x1 = AVG_K(X, i1, i2, j1, j2, k1), x0 = AVG_K(X, i1, i2, j1, j2, ke);
         double y2 = AVG_K(Y, i1, i2, j1, j2, k2), y1 = AVG_K(Y, i1, i2, j1, j2, k1), y0 = AVG_K(Y, i1, i2, j1, j2, ke);
         double z2 = AVG_K(Z, i1, i2, j1, j2, k2), z1 = AVG_K(Z, i1, i2, j1, j2, k1), z0 = AVG_K(Z, i1, i2, j1, j2, ke);
@@ -212,7 +218,7 @@ __global__ void k_metric_zet(Nodes N, Geom g, int s, double inv_pot, double* g31
         yzet = .5 * (3. * y0 - 4. * y1 + y2);
         zzet = .5 * (3. * z0 - 4. * z1 + z2);
     } else {
-        const int k2 = (k + 1) * s, k1 = (k - 1) * s;
+        const int k2 = (k + 1) * sz, k1 = (k - 1) * sz;
         double xav = AVG_K(X, i1, i2, j1, j2, k2), xdt = AVG_K(X, i1, i2, j1, j2, k1);
         double yav = AVG_K(Y, i1, i2, j1, j2, k2), ydt = AVG_K(Y, i1, i2, j1, j2, k1);
         double zav = AVG_K(Z, i1, i2, j1, j2, k2), zdt = AVG_K(Z, i1, i2, j1, j2, k1);
@@ -229,7 +235,7 @@ __global__ void k_metric_zet(Nodes N, Geom g, int s, double inv_pot, double* g31
     double t[3];
     metric_row(2, xcsi, ycsi, zcsi, xeta, yeta, zeta, xzet, yzet, zzet, t);
     const long long q = g.at(i, j, k);
-    if (s == 1) {
+    if (sx == 1 && sy == 1 && sz == 1) {
         g31[q] = t[0]; g32[q] = t[1]; g33[q] = t[2];
     } else {
         g31[q] = t[0] * inv_pot; g32[q] = t[1] * inv_pot; g33[q] = t[2] * inv_pot;
@@ -237,18 +243,16 @@ __global__ void k_metric_zet(Nodes N, Geom g, int s, double inv_pot, double* g31
 }
 
 cudaError_t launch_metric(const double* xn, const double* yn, const double* zn, int jx, int jy, int jz,
-                          int ip, int jp, int kp, int level, Geom g, double* const gout[9],
-                          cudaStream_t st) {
+                          int ip, int jp, int kp, int sx, int sy, int sz, double inv_div, Geom g,
+                          double* const gout[9], cudaStream_t st) {
     Nodes N{xn, yn, zn, jx, jy, jz, ip, jp, kp};
-    const int s = 1 << (level - 1);
-    const double inv_pot = 1.0 / (double)s;
     dim3 blk(32, 4);
-    k_metric_csi<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 3) / 4, g.nz), blk, 0, st>>>(N, g, s, inv_pot, gout[0],
-                                                                                   gout[1], gout[2]);
-    k_metric_eta<<<dim3((g.nx + 31) / 32, (g.ny + 1 + 3) / 4, g.nz), blk, 0, st>>>(N, g, s, inv_pot, gout[3],
-                                                                                   gout[4], gout[5]);
-    k_metric_zet<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz + 1), blk, 0, st>>>(N, g, s, inv_pot, gout[6],
-                                                                                   gout[7], gout[8]);
+    k_metric_csi<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 3) / 4, g.nz), blk, 0, st>>>(N, g, sx, sy, sz, inv_div,
+                                                                                   gout[0], gout[1], gout[2]);
+    k_metric_eta<<<dim3((g.nx + 31) / 32, (g.ny + 1 + 3) / 4, g.nz), blk, 0, st>>>(N, g, sx, sy, sz, inv_div,
+                                                                                   gout[3], gout[4], gout[5]);
+    k_metric_zet<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz + 1), blk, 0, st>>>(N, g, sx, sy, sz, inv_div,
+                                                                                   gout[6], gout[7], gout[8]);
     return cudaGetLastError();
 }
 

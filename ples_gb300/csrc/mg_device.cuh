@@ -17,7 +17,15 @@
 //   A1 = g11*ppot2,  B12 = g12*ppot2/4,  B13 = g13*ppot2/4   (csi faces)
 //   A2 = g22*ppot2,  B21 = g21*ppot2/4,  B23 = g23*ppot2/4   (eta faces)
 //   A3 = g33*ppot2,  B31 = g31*ppot2/4,  B32 = g32*ppot2/4   (zeta faces)
-// with ppot2 = 4^-(n-1).
+// With the coarse metric t of a level built from nodes sub-sampled by the
+// cumulative strides (sx,sy,sz), the stored coefficient is t/(sx*sy*sz):
+// for the reference's full coarsening (sx=sy=sz=2^(n-1)) that is exactly
+// mul_met's t/pot times ppot2.
+//
+// Periodic ghost shell (ip = kp = 0).  Ghost cells with i or k outside the
+// interior hold the periodic image of the interior, for every row j
+// including the two wall ghost rows; every kernel that writes a field keeps
+// the shell consistent, so no separate ghost-copy pass is needed.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -56,6 +64,29 @@ struct Coef {
 template <typename T>
 __device__ __forceinline__ T ld(const T* p, long long q) { return __ldg(p + q); }
 
+// Store v at interior cell (i,j,k) and at its periodic images in the x/z
+// ghost shell (the reference's periodic copies, corner lines, vertical frame
+// and horizontal square, multigrid.f03:1145-1158, 1325-1620).
+template <typename T>
+__device__ __forceinline__ void store_periodic(const Geom& g, T* p, int i, int j, int k, T v) {
+    p[g.at(i, j, k)] = v;
+    const int gi = i == g.nx ? 0 : (i == 1 ? g.nx + 1 : -1);
+    const int gk = k == g.nz ? 0 : (k == 1 ? g.nz + 1 : -1);
+    if (gi >= 0) p[g.at(gi, j, k)] = v;
+    if (gk >= 0) {
+        p[g.at(i, j, gk)] = v;
+        if (gi >= 0) p[g.at(gi, j, gk)] = v;
+    }
+    if (g.nx == 1 && i == 1) {  // a single column is its own image on both sides
+        p[g.at(0, j, k)] = v;
+        if (gk >= 0) p[g.at(0, j, gk)] = v;
+    }
+    if (g.nz == 1 && k == 1) {
+        p[g.at(i, j, 0)] = v;
+        if (gi >= 0) p[g.at(gi, j, 0)] = v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // L_n(p) - rh at one interior cell: resid_sndrcv.f03:80-151 with the scaled
 // coefficients.  The six face fluxes are res_dx, res_sn, res_sop, res_sot,
@@ -84,12 +115,9 @@ __device__ __forceinline__ T cell_residual(const Geom& g, const Coef<T>& c, cons
 }
 
 // ---------------------------------------------------------------------------
-// Periodic ghost shell in x and z (ip = kp = 0): every ghost cell with i or k
-// outside the interior copies its periodic image, for all rows j = 0..ny+1
-// including the wall ghost rows.  At the fixed point this is exactly the
-// reference's x/z copies, corner lines, vertical frame and horizontal square
-// (multigrid.f03:1145-1158, 1325-1620).  Sources are never ghosts in x or z,
-// so the kernel is race-free.
+// Periodic ghost shell refresh (ip = kp = 0): every ghost cell with i or k
+// outside the interior copies its periodic image, rows j = 0..ny+1.  Used
+// once on fields that arrive from outside (the caller's fi).
 template <typename T>
 __global__ void k_ghost_xz(Geom g, T* __restrict__ p) {
     const int nxg = g.nx + 2, nyg = g.ny + 2;
@@ -120,121 +148,301 @@ __global__ void k_ghost_xz(Geom g, T* __restrict__ p) {
 }
 
 // ---------------------------------------------------------------------------
-// eta-line relaxation (the device form of solut_sndrcv_slor,
-// multigrid.f03:1939-2290 with tridag.f03).  One thread owns the line (i,k)
-// and solves the tridiagonal system over j = 0..ny+1, whose end rows are the
-// wall ghost relations (sett.f03:114-143): off-line neighbours and all cross
-// terms are explicit, the normal x/z couplings sit on the diagonal.
-//   ZEBRA = false: Jacobi over lines, pin -> pout, pout = pin + omega*(x - pin)
-//   ZEBRA = true : lines with (i%2, k%2) == colour, in place, SOR factor omega
-// The homogeneous wall relation is used (an = 0): this kernel runs on
-// corrections only; the FP64 outer loop applies the cs terms.
-// Shared memory holds c'(j), d'(j) of the Thomas sweep, [j][thread].
-template <typename T, bool ZEBRA>
-__global__ void k_line_relax(Geom g, Coef<T> c, const T* pin, T* pout,
-                             const T* __restrict__ rh, T omega, int colour) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nth = blockDim.x * blockDim.y;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    T* sc = reinterpret_cast<T*>(smem_raw);
-    T* sd = sc + (size_t)(g.ny + 2) * nth;
-    int i, k;
-    if (ZEBRA) {
-        i = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + 1 + (colour & 1);
-        k = 2 * (blockIdx.y * blockDim.y + threadIdx.y) + 1 + (colour >> 1);
-    } else {
-        i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-        k = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    }
-    if (i > g.nx || k > g.nz) return;
-    const int ny = g.ny;
+// One row of the eta-line system of line (i,k) (solut_sndrcv_slor,
+// multigrid.f03:2126-2198 with sett.f03:114-143).  Rows 0 and ny+1 are the
+// wall ghost relations (homogeneous, an = 0: the smoother runs on
+// corrections; the FP64 outer loop applies the cs terms):
+//   row 0     : A2(0) p0 - A2(0) p1             = B21(0) X0 + B23(0) Z0
+//   row j     : A2(j-1) p(j-1) + b p(j) + A2(j) p(j+1) = rh - N(off-line)
+//   row ny+1  : -A2(ny) p(ny) + A2(ny) p(ny+1)  = -(B21(ny) X + B23(ny) Z)
+// with b = -(A2(j)+A2(j-1)+A1(i)+A1(i-1)+A3(k)+A3(k-1)); every off-line
+// neighbour and every cross term is explicit.  Outputs: f, the diagonal b
+// and a2 = A2 of face j (the coupling of rows j and j+1).  ZERO: p == 0.
+template <typename T, bool ZERO>
+__device__ __forceinline__ void line_row(const Geom& g, const Coef<T>& c, const T* __restrict__ p,
+                                         const T* __restrict__ rh, int i, int j, int k, T& f, T& b, T& a2) {
     const long long sj = g.sj, sk = g.sk;
-    const T* p = pin;
-
-    // x/z normal couplings of this line's cells go on the diagonal
-    // row 0: bottom wall ghost relation (mul_boun_sndrcv :1166-1173, an = 0)
-    long long q = g.at(i, 0, k);
-    T a2 = ld(c.a2, q);
-    T f = ld(c.b21, q) * (ld(p, q + 1 + sj) + ld(p, q + 1) - ld(p, q - 1 + sj) - ld(p, q - 1)) +
-          ld(c.b23, q) * (ld(p, q + sj + sk) + ld(p, q + sk) - ld(p, q + sj - sk) - ld(p, q - sk));
-    T cp = T(-1);         // c'_0 = c_0 / b_0 = -a2 / a2
-    T dp = f / a2;        // d'_0
-    sc[tid] = cp;
-    sd[tid] = dp;
-    T a2m = a2;           // A2 of face j-1
-    for (int j = 1; j <= ny; ++j) {
-        q += sj;
-        const T pc = ld(p, q);
-        const T pe = ld(p, q + 1), pw = ld(p, q - 1);
-        const T pn = ld(p, q + sj), ps = ld(p, q - sj);
-        const T pf = ld(p, q + sk), pb = ld(p, q - sk);
-        const T pen = ld(p, q + 1 + sj), pes = ld(p, q + 1 - sj), pwn = ld(p, q - 1 + sj), pws = ld(p, q - 1 - sj);
-        const T pef = ld(p, q + 1 + sk), peb = ld(p, q + 1 - sk), pwf = ld(p, q - 1 + sk), pwb = ld(p, q - 1 - sk);
-        const T pnf = ld(p, q + sj + sk), pnb = ld(p, q + sj - sk), psf = ld(p, q - sj + sk), psb = ld(p, q - sj - sk);
-        const T a1e = ld(c.a1, q), a1w = ld(c.a1, q - 1);
-        const T a3f = ld(c.a3, q), a3b = ld(c.a3, q - sk);
+    const long long q = g.at(i, j, k);
+    if (j == 0) {
         a2 = ld(c.a2, q);
-        // off-line explicit part N (cross terms use the old on-line values too)
-        T nsum = a1e * pe + a1w * pw + a3f * pf + a3b * pb;
-        nsum += ld(c.b12, q) * (pen + pn - pes - ps) - ld(c.b12, q - 1) * (pn + pwn - ps - pws);
-        nsum += ld(c.b13, q) * (pef + pf - peb - pb) - ld(c.b13, q - 1) * (pf + pwf - pb - pwb);
-        nsum += ld(c.b21, q) * (pen + pe - pwn - pw) - ld(c.b21, q - sj) * (pe + pes - pw - pws);
-        nsum += ld(c.b23, q) * (pnf + pf - pnb - pb) - ld(c.b23, q - sj) * (pf + psf - pb - psb);
-        nsum += ld(c.b31, q) * (pef + pe - pwf - pw) - ld(c.b31, q - sk) * (pe + peb - pw - pwb);
-        nsum += ld(c.b32, q) * (pnf + pn - psf - ps) - ld(c.b32, q - sk) * (pn + pnb - ps - psb);
-        f = ld(rh, q) - nsum;
-        const T b = -(a2 + a2m + a1e + a1w + a3f + a3b);
-        const T m = b - a2m * cp;
-        const T inv = T(1) / m;
-        cp = a2 * inv;
-        dp = (f - a2m * dp) * inv;
-        sc[(size_t)j * nth + tid] = cp;
-        sd[(size_t)j * nth + tid] = dp;
-        a2m = a2;
+        b = a2;
+        f = ZERO ? T(0)
+                 : ld(c.b21, q) * (ld(p, q + 1 + sj) + ld(p, q + 1) - ld(p, q - 1 + sj) - ld(p, q - 1)) +
+                       ld(c.b23, q) * (ld(p, q + sj + sk) + ld(p, q + sk) - ld(p, q + sj - sk) - ld(p, q - sk));
+        return;
     }
-    // row ny+1: top wall ghost relation (mul_boun_sndrcv :1175-1186, an = 0)
-    q += sj;
+    if (j == g.ny + 1) {
+        const long long qn = q - sj;
+        a2 = T(0);
+        b = ld(c.a2, qn);
+        f = ZERO ? T(0)
+                 : -(ld(c.b21, qn) * (ld(p, q + 1) + ld(p, qn + 1) - ld(p, q - 1) - ld(p, qn - 1)) +
+                     ld(c.b23, qn) * (ld(p, q + sk) + ld(p, qn + sk) - ld(p, q - sk) - ld(p, qn - sk)));
+        return;
+    }
+    const T a1e = ld(c.a1, q), a1w = ld(c.a1, q - 1);
+    const T a3f = ld(c.a3, q), a3b = ld(c.a3, q - sk);
+    a2 = ld(c.a2, q);
+    b = -(a2 + ld(c.a2, q - sj) + a1e + a1w + a3f + a3b);
+    if (ZERO) {
+        f = ld(rh, q);
+        return;
+    }
+    const T pe = ld(p, q + 1), pw = ld(p, q - 1);
+    const T pn = ld(p, q + sj), ps = ld(p, q - sj);
+    const T pf = ld(p, q + sk), pb = ld(p, q - sk);
+    const T pen = ld(p, q + 1 + sj), pes = ld(p, q + 1 - sj), pwn = ld(p, q - 1 + sj), pws = ld(p, q - 1 - sj);
+    const T pef = ld(p, q + 1 + sk), peb = ld(p, q + 1 - sk), pwf = ld(p, q - 1 + sk), pwb = ld(p, q - 1 - sk);
+    const T pnf = ld(p, q + sj + sk), pnb = ld(p, q + sj - sk), psf = ld(p, q - sj + sk), psb = ld(p, q - sj - sk);
+    T nsum = a1e * pe + a1w * pw + a3f * pf + a3b * pb;
+    nsum += ld(c.b12, q) * (pen + pn - pes - ps) - ld(c.b12, q - 1) * (pn + pwn - ps - pws);
+    nsum += ld(c.b13, q) * (pef + pf - peb - pb) - ld(c.b13, q - 1) * (pf + pwf - pb - pwb);
+    nsum += ld(c.b21, q) * (pen + pe - pwn - pw) - ld(c.b21, q - sj) * (pe + pes - pw - pws);
+    nsum += ld(c.b23, q) * (pnf + pf - pnb - pb) - ld(c.b23, q - sj) * (pf + psf - pb - psb);
+    nsum += ld(c.b31, q) * (pef + pe - pwf - pw) - ld(c.b31, q - sk) * (pe + peb - pw - pwb);
+    nsum += ld(c.b32, q) * (pnf + pn - psf - ps) - ld(c.b32, q - sk) * (pn + pnb - ps - psb);
+    f = ld(rh, q) - nsum;
+}
+
+template <typename T>
+__device__ __forceinline__ T rcp(T x) { return T(1) / x; }
+
+// Thomas sweep over rows 0..ny+1 held in shared arrays with stride `st`:
+// f (in: right-hand side, out: solution), b (in: diagonal, scratch), a2
+// (A2 of face j).  tridag.f03:2-32 on the system described at line_row.
+template <typename T>
+__device__ __forceinline__ void thomas(int ny, T* f, T* b, const T* a2, int st) {
+    T cp = T(-1);  // c'_0 = -A2(0)/A2(0)
+    T dp = f[0] / b[0];
+    b[0] = cp;
+    f[0] = dp;
+    for (int j = 1; j <= ny; ++j) {
+        const T a = a2[(j - 1) * st], cc = a2[j * st];
+        const T inv = rcp(b[j * st] - a * cp);
+        cp = cc * inv;
+        dp = (f[j * st] - a * dp) * inv;
+        b[j * st] = cp;
+        f[j * st] = dp;
+    }
     {
-        const long long qn = q - sj;  // face ny lives at cell (i, ny, k)
-        f = -(ld(c.b21, qn) * (ld(p, q + 1) + ld(p, qn + 1) - ld(p, q - 1) - ld(p, qn - 1)) +
-              ld(c.b23, qn) * (ld(p, q + sk) + ld(p, qn + sk) - ld(p, q - sk) - ld(p, qn - sk)));
-        // a = -A2(ny), b = A2(ny), c = 0
-        const T m = a2m - (-a2m) * cp;
-        dp = (f + a2m * dp) / m;
+        const T a = -a2[ny * st];  // row ny+1: sub-diagonal -A2(ny), diagonal A2(ny)
+        const T x = (f[(ny + 1) * st] - a * dp) / (b[(ny + 1) * st] - a * cp);
+        f[(ny + 1) * st] = x;
+        T xs = x;
+        for (int j = ny; j >= 0; --j) {
+            xs = f[j * st] - b[j * st] * xs;
+            f[j * st] = xs;
+        }
     }
-    // back substitution and relaxed update, j = ny+1 .. 0
-    T xs = dp;
-    {
-        const T old = ld(p, q);
-        pout[q] = old + omega * (xs - old);
+}
+
+// ---------------------------------------------------------------------------
+// LU factor of the fixed eta-line operator (sett.f03:114-143 rows, the
+// forward sweep of tridag.f03): c'(0) = -1, c'(j) = A2(j) / (b(j) - A2(j-1)
+// c'(j-1)).  The operator depends on the coefficients only, so c' is built
+// once per level; the smoothers then need one division per row in their
+// parallel phase and a pure FMA chain in the sequential one.
+template <typename T>
+__global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int k = blockIdx.y + 1;
+    if (i > g.nx) return;
+    T prev = T(-1);
+    cp[g.at(i, 0, k)] = prev;
+    for (int j = 1; j <= g.ny; ++j) {
+        const long long q = g.at(i, j, k);
+        const T a = ld(c.a2, q - g.sj), cc = ld(c.a2, q);
+        const T b = -(cc + a + ld(c.a1, q) + ld(c.a1, q - 1) + ld(c.a3, q) + ld(c.a3, q - g.sk));
+        prev = cc / (b - a * prev);
+        cp[q] = prev;
     }
-    for (int j = ny; j >= 0; --j) {
-        q -= sj;
-        xs = sd[(size_t)j * nth + tid] - sc[(size_t)j * nth + tid] * xs;
-        const T old = ld(p, q);
-        pout[q] = old + omega * (xs - old);
+    cp[g.at(i, g.ny + 1, k)] = T(0);
+}
+
+// ---------------------------------------------------------------------------
+// eta-line relaxation (the device form of solut_sndrcv_slor,
+// multigrid.f03:1939-2290, with tridag.f03).  A CTA owns 32 consecutive
+// lines in i (one per lane) of one plane k, all rows j = 0..ny+1:
+//   phase 1: every warp builds rows j = w, w+W, ... of its lines' systems
+//            (coalesced row loads; off-line neighbours and cross terms
+//            explicit) and stores g = f/m, alpha = a/m, c' (m = b - a c'(j-1))
+//   phase 2: warp 0 runs the two FMA recurrences per line in shared memory
+//   phase 3: every warp writes its rows, relaxed, with the periodic images.
+// JACOBI: all lines of all planes from the old field pin -> pout.
+// ZEBRA : the lines with one parity of k (launch argument kpar); inside the
+//         CTA the even-i lines first, then the odd-i lines, which see the new
+//         even-i neighbours of the same tile (Gauss-Seidel in x and z as the
+//         reference's lexicographic line SOR, Jacobi only across tile edges).
+//         Phase 1 still reads every row once for all 32 lanes: the odd-i
+//         lanes keep f without its six in-plane x-neighbour terms, which are
+//         added after the even-i update (4 coefficient arrays re-read).
+//         Own-plane old values come from pin, k+-1 planes from pk (= pin for
+//         the first parity, = pout for the second); output to pout.
+// ZIN: pin is identically zero (first sweep of a correction); zk: pk is too.
+// Shared memory: 3 arrays [ny+2][32].
+template <typename T, bool ZEBRA, bool ZIN>
+__global__ void __launch_bounds__(256) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
+                                                    const T* __restrict__ pin, const T* __restrict__ pk,
+                                                    T* __restrict__ pout, const T* __restrict__ rh, T omega,
+                                                    int kpar, int zk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nj = g.ny + 2, ny = g.ny;
+    T* G = reinterpret_cast<T*>(smem_raw);
+    T* AL = G + nj * 32;
+    T* CP = AL + nj * 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int k = ZEBRA ? 2 * blockIdx.x + 1 + kpar : blockIdx.x + 1;
+    if (k > g.nz) return;
+    const int i = blockIdx.y * 32 + lane + 1;
+    const bool act = i <= g.nx;
+    const bool odd = ZEBRA && (i & 1);  // updated in the second half
+    const long long sj = g.sj, sk = g.sk;
+    // old neighbour value at (i+di, j+dj, k+dk)
+    auto P = [&](int j, int di, int dj, int dk) -> T {
+        const long long q = g.at(i + di, j + dj, k + dk);
+        if (dk != 0) return zk ? T(0) : ld(pk, q);
+        return ZIN ? T(0) : ld(pin, q);
+    };
+    // in-plane x-neighbour after the even-i update (odd lanes, second half)
+    auto PX = [&](int j, int di, int dj) -> T {
+        const int l2 = lane + di;
+        if (l2 >= 0 && l2 < 32 && i + di >= 1 && i + di <= g.nx) return G[(j + dj) * 32 + l2];
+        return ZIN ? T(0) : ld(pin, g.at(i + di, j + dj, k));
+    };
+    const bool noneigh = ZIN && (!ZEBRA || zk);  // every old neighbour is zero
+    if (act) {
+        for (int j = w; j < nj; j += nw) {
+            const long long q = g.at(i, j, k);
+            T f, a, im;
+            if (j == 0) {
+                const T a2 = ld(c.a2, q);
+                f = noneigh ? T(0)
+                            : ld(c.b23, q) * (P(j, 0, 1, 1) + P(j, 0, 0, 1) - P(j, 0, 1, -1) - P(j, 0, 0, -1));
+                if (!odd && !noneigh)
+                    f += ld(c.b21, q) * (P(j, 1, 1, 0) + P(j, 1, 0, 0) - P(j, -1, 1, 0) - P(j, -1, 0, 0));
+                a = T(0);
+                im = T(1) / a2;
+            } else if (j == ny + 1) {
+                const long long qn = q - sj;
+                const T a2 = ld(c.a2, qn);
+                f = noneigh ? T(0)
+                            : -(ld(c.b23, qn) * (P(j, 0, 0, 1) + P(j, 0, -1, 1) - P(j, 0, 0, -1) - P(j, 0, -1, -1)));
+                if (!odd && !noneigh)
+                    f -= ld(c.b21, qn) * (P(j, 1, 0, 0) + P(j, 1, -1, 0) - P(j, -1, 0, 0) - P(j, -1, -1, 0));
+                a = -a2;
+                im = T(1) / (a2 - a * ld(cpa, qn));
+            } else {
+                const T a1e = ld(c.a1, q), a1w = ld(c.a1, q - 1);
+                const T a3f = ld(c.a3, q), a3b = ld(c.a3, q - sk);
+                const T a2 = ld(c.a2, q);
+                a = ld(c.a2, q - sj);
+                const T b = -(a2 + a + a1e + a1w + a3f + a3b);
+                im = T(1) / (b - a * ld(cpa, q - sj));
+                f = ld(rh, q);
+                if (!noneigh) {
+                    const T pn = P(j, 0, 1, 0), ps = P(j, 0, -1, 0);
+                    const T pf = P(j, 0, 0, 1), pb = P(j, 0, 0, -1);
+                    const T pef = P(j, 1, 0, 1), peb = P(j, 1, 0, -1), pwf = P(j, -1, 0, 1), pwb = P(j, -1, 0, -1);
+                    const T pnf = P(j, 0, 1, 1), pnb = P(j, 0, 1, -1), psf = P(j, 0, -1, 1), psb = P(j, 0, -1, -1);
+                    const T b12 = ld(c.b12, q), b12w = ld(c.b12, q - 1);
+                    const T b31 = ld(c.b31, q), b31b = ld(c.b31, q - sk);
+                    // every term without an in-plane x-neighbour
+                    T rest = a3f * pf + a3b * pb + (b12 - b12w) * (pn - ps);
+                    rest += ld(c.b13, q) * (pef + pf - peb - pb) - ld(c.b13, q - 1) * (pf + pwf - pb - pwb);
+                    rest += ld(c.b23, q) * (pnf + pf - pnb - pb) - ld(c.b23, q - sj) * (pf + psf - pb - psb);
+                    rest += b31 * (pef - pwf) - b31b * (peb - pwb);
+                    rest += ld(c.b32, q) * (pnf + pn - psf - ps) - ld(c.b32, q - sk) * (pn + pnb - ps - psb);
+                    f -= rest;
+                    if (!odd) {  // the in-plane x-neighbour terms, old values
+                        const T pe = P(j, 1, 0, 0), pw = P(j, -1, 0, 0);
+                        const T pen = P(j, 1, 1, 0), pes = P(j, 1, -1, 0), pwn = P(j, -1, 1, 0), pws = P(j, -1, -1, 0);
+                        const T b21 = ld(c.b21, q), b21s = ld(c.b21, q - sj);
+                        const T tx = a1e * pe + a1w * pw + b12 * (pen - pes) - b12w * (pwn - pws) +
+                                     b21 * (pen + pe - pwn - pw) - b21s * (pe + pes - pw - pws) +
+                                     (b31 - b31b) * (pe - pw);
+                        f -= tx;
+                    }
+                }
+            }
+            G[j * 32 + lane] = f * im;
+            AL[j * 32 + lane] = a * im;
+            // odd lanes keep 1/m here until their x-neighbour terms are added
+            CP[j * 32 + lane] = odd ? im : (j == ny + 1 ? T(0) : ld(cpa, q));
+        }
+    }
+    const int nhalf = ZEBRA ? 2 : 1;
+    for (int half = 0; half < nhalf; ++half) {
+        const bool mine = act && (!ZEBRA || ((i & 1) == half));
+        if (ZEBRA && half == 1 && mine) {  // in-plane x-neighbour terms with the new even-i values
+            for (int j = w; j < nj; j += nw) {
+                const long long q = g.at(i, j, k);
+                T tx;
+                if (j == 0) {
+                    tx = -ld(c.b21, q) * (PX(j, 1, 1) + PX(j, 1, 0) - PX(j, -1, 1) - PX(j, -1, 0));
+                } else if (j == ny + 1) {
+                    tx = ld(c.b21, q - sj) * (PX(j, 1, 0) + PX(j, 1, -1) - PX(j, -1, 0) - PX(j, -1, -1));
+                } else {
+                    const T pe = PX(j, 1, 0), pw = PX(j, -1, 0);
+                    const T pen = PX(j, 1, 1), pes = PX(j, 1, -1), pwn = PX(j, -1, 1), pws = PX(j, -1, -1);
+                    const T b12 = ld(c.b12, q), b12w = ld(c.b12, q - 1);
+                    tx = ld(c.a1, q) * pe + ld(c.a1, q - 1) * pw + b12 * (pen - pes) - b12w * (pwn - pws) +
+                         ld(c.b21, q) * (pen + pe - pwn - pw) - ld(c.b21, q - sj) * (pe + pes - pw - pws) +
+                         (ld(c.b31, q) - ld(c.b31, q - sk)) * (pe - pw);
+                }
+                const T im = CP[j * 32 + lane];
+                G[j * 32 + lane] -= tx * im;
+                CP[j * 32 + lane] = j == ny + 1 ? T(0) : ld(cpa, q);
+            }
+        }
+        __syncthreads();
+        if (w == 0 && mine) {
+            T d = G[lane];
+            for (int j = 1; j < nj; ++j) {
+                d = G[j * 32 + lane] - AL[j * 32 + lane] * d;
+                G[j * 32 + lane] = d;
+            }
+            T x = d;
+            for (int j = nj - 2; j >= 0; --j) {
+                x = G[j * 32 + lane] - CP[j * 32 + lane] * x;
+                G[j * 32 + lane] = x;
+            }
+        }
+        __syncthreads();
+        if (mine) {
+            for (int j = w; j < nj; j += nw) {
+                const T x = G[j * 32 + lane];
+                T v;
+                if (ZIN) {
+                    v = omega * x;
+                } else {
+                    const T old = ld(pin, g.at(i, j, k));
+                    v = old + omega * (x - old);
+                }
+                if (ZEBRA) G[j * 32 + lane] = v;
+                store_periodic(g, pout, i, j, k, v);
+            }
+        }
+        if (ZEBRA) __syncthreads();
     }
 }
 
 // ---------------------------------------------------------------------------
 // Residual + restriction (resid_sndrcv.f03 followed by restrict_sndrcv.f03:
-// 32-53): coarse rh = -(1/8) * sum of the 8 fine residuals L(p) - rh.
+// 32-53) for a coarsening ratio (rx,ry,rz) in {1,2}^3: coarse rh =
+// -(1/(rx*ry*rz)) * sum of the fine residuals L(p) - rh of its children.
 template <typename T>
 __global__ void k_resid_restrict(Geom gf, Geom gc, Coef<T> c, const T* __restrict__ p,
-                                 const T* __restrict__ rh, T* __restrict__ rhc) {
+                                 const T* __restrict__ rh, T* __restrict__ rhc, int rx, int ry, int rz) {
     const int ic = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int jc = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int kc = blockIdx.z + 1;
     if (ic > gc.nx || jc > gc.ny) return;
     T s = T(0);
-#pragma unroll
-    for (int dk = -1; dk <= 0; ++dk)
-#pragma unroll
-        for (int dj = -1; dj <= 0; ++dj)
-#pragma unroll
-            for (int di = -1; di <= 0; ++di)
-                s += cell_residual(gf, c, p, rh, gf.at(2 * ic + di, 2 * jc + dj, 2 * kc + dk));
-    rhc[gc.at(ic, jc, kc)] = -s * T(0.125);
+    for (int dk = 0; dk < rz; ++dk)
+        for (int dj = 0; dj < ry; ++dj)
+            for (int di = 0; di < rx; ++di)
+                s += cell_residual(gf, c, p, rh, gf.at(rx * ic - di, ry * jc - dj, rz * kc - dk));
+    rhc[gc.at(ic, jc, kc)] = -s / T(rx * ry * rz);
 }
 
 // Plain residual L(p) - rh into out (interior cells).
@@ -249,51 +457,89 @@ __global__ void k_residual(Geom g, Coef<T> c, const T* __restrict__ p, const T* 
     out[q] = cell_residual(g, c, p, rh, q);
 }
 
-// Restriction alone (restrict_sndrcv.f03:32-53).
+// Restriction alone (restrict_sndrcv.f03:32-53), summed in the reference's
+// order for full coarsening.
 template <typename T>
-__global__ void k_restrict(Geom gf, Geom gc, const T* __restrict__ r, T* __restrict__ rc) {
+__global__ void k_restrict(Geom gf, Geom gc, const T* __restrict__ r, T* __restrict__ rc, int rx, int ry, int rz) {
     const int ic = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int jc = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int kc = blockIdx.z + 1;
     if (ic > gc.nx || jc > gc.ny) return;
-    const int id = 2 * ic, jd = 2 * jc, kd = 2 * kc;
-    T v = r[gf.at(id, jd, kd)] + r[gf.at(id - 1, jd, kd)] + r[gf.at(id, jd - 1, kd)] +
-          r[gf.at(id - 1, jd - 1, kd)] + r[gf.at(id, jd, kd - 1)] + r[gf.at(id - 1, jd, kd - 1)] +
-          r[gf.at(id, jd - 1, kd - 1)] + r[gf.at(id - 1, jd - 1, kd - 1)];
-    rc[gc.at(ic, jc, kc)] = -v * T(0.125);
+    const int id = rx * ic, jd = ry * jc, kd = rz * kc;
+    T v;
+    if (rx == 2 && ry == 2 && rz == 2) {
+        v = r[gf.at(id, jd, kd)] + r[gf.at(id - 1, jd, kd)] + r[gf.at(id, jd - 1, kd)] +
+            r[gf.at(id - 1, jd - 1, kd)] + r[gf.at(id, jd, kd - 1)] + r[gf.at(id - 1, jd, kd - 1)] +
+            r[gf.at(id, jd - 1, kd - 1)] + r[gf.at(id - 1, jd - 1, kd - 1)];
+        rc[gc.at(ic, jc, kc)] = -v * T(0.125);
+        return;
+    }
+    v = T(0);
+    for (int dk = 0; dk < rz; ++dk)
+        for (int dj = 0; dj < ry; ++dj)
+            for (int di = 0; di < rx; ++di) v += r[gf.at(id - di, jd - dj, kd - dk)];
+    rc[gc.at(ic, jc, kc)] = -v / T(rx * ry * rz);
 }
 
 // ---------------------------------------------------------------------------
-// Prolongation (prolong.f03:64-261): coarse cells i = 0..nxc, j = 0..nyc,
-// k = 0..nzc add trilinear (27/9/3/1)/64 corrections into their eight fine
-// children (2i+a, 2j+b, 2k+c), which cover every fine cell including ghosts.
+// Prolongation (prolong.f03:64-261): every fine cell, ghosts included, adds
+// the tensor-product linear interpolation of the coarse correction; along a
+// coarsened direction fine 2c gets (3/4, 1/4) of coarse (c, c+1) and fine
+// 2c+1 gets (1/4, 3/4) -- the reference's (27/9/3/1)/64 weights for full
+// coarsening; along an uncoarsened direction the coarse value is copied.
 template <typename Tf, typename Tc>
-__global__ void k_prolong(Geom gf, Geom gc, Tf* __restrict__ pf, const Tc* __restrict__ pc) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i > gc.nx || j > gc.ny) return;
-    const long long q = gc.at(i, j, k);
-    const long long sj = gc.sj, sk = gc.sk;
-    Tc v[8];
-    v[0] = pc[q]; v[1] = pc[q + 1]; v[2] = pc[q + sj]; v[3] = pc[q + 1 + sj];
-    v[4] = pc[q + sk]; v[5] = pc[q + 1 + sk]; v[6] = pc[q + sj + sk]; v[7] = pc[q + 1 + sj + sk];
-#pragma unroll
-    for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-        for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-            for (int cx = 0; cx < 2; ++cx) {
-                Tc s = Tc(0);
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    const int ox = c & 1, oy = (c >> 1) & 1, oz = c >> 2;
-                    const Tc w = Tc((ox == cx ? 3 : 1) * (oy == cy ? 3 : 1) * (oz == cz ? 3 : 1));
-                    s += w * v[c];
-                }
-                const long long qf = gf.at(2 * i + cx, 2 * j + cy, 2 * k + cz);
-                pf[qf] = pf[qf] + Tf(s * Tc(1.0 / 64.0));
-            }
+__global__ void k_prolong(Geom gf, Geom gc, Tf* __restrict__ pf, const Tc* __restrict__ pc, int rx, int ry,
+                          int rz) {
+    const int fi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int fj = blockIdx.y * blockDim.y + threadIdx.y;
+    const int fk = blockIdx.z;
+    if (fi > gf.nx + 1 || fj > gf.ny + 1) return;
+    int ci[2], cj[2], ck[2];
+    Tc wi[2], wj[2], wk[2];
+    int ni = 1, nj = 1, nk = 1;
+    if (rx == 2) { ci[0] = fi >> 1; ci[1] = ci[0] + 1; wi[0] = (fi & 1) ? Tc(0.25) : Tc(0.75); wi[1] = Tc(1) - wi[0]; ni = 2; }
+    else { ci[0] = fi; wi[0] = Tc(1); }
+    if (ry == 2) { cj[0] = fj >> 1; cj[1] = cj[0] + 1; wj[0] = (fj & 1) ? Tc(0.25) : Tc(0.75); wj[1] = Tc(1) - wj[0]; nj = 2; }
+    else { cj[0] = fj; wj[0] = Tc(1); }
+    if (rz == 2) { ck[0] = fk >> 1; ck[1] = ck[0] + 1; wk[0] = (fk & 1) ? Tc(0.25) : Tc(0.75); wk[1] = Tc(1) - wk[0]; nk = 2; }
+    else { ck[0] = fk; wk[0] = Tc(1); }
+    Tc s = Tc(0);
+    for (int c = 0; c < nk; ++c)
+        for (int b = 0; b < nj; ++b)
+            for (int a = 0; a < ni; ++a) s += wi[a] * wj[b] * wk[c] * pc[gc.at(ci[a], cj[b], ck[c])];
+    const long long q = gf.at(fi, fj, fk);
+    pf[q] = pf[q] + Tf(s);
+}
+
+// ---------------------------------------------------------------------------
+// Exact solve on the coarsest level: e = S r with S the (pre-computed)
+// inverse of the bordered coarse system (interior cells and wall ghost rows
+// as unknowns; mean of e zero, incompatible part of r absorbed).  Unknown u
+// = ((k-1)*nx + (i-1))*(ny+2) + j.  Each CTA stages r in shared memory; one
+// warp per row of S.
+template <typename T>
+__global__ void k_dense_solve(Geom g, const T* __restrict__ S, const T* __restrict__ rh, T* __restrict__ p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* r = reinterpret_cast<T*>(smem_raw);
+    const int nj = g.ny + 2;
+    const int n = g.nx * g.nz * nj;
+    for (int u = threadIdx.x; u < n; u += blockDim.x) {
+        const int j = u % nj, col = u / nj;
+        const int i = col % g.nx + 1, k = col / g.nx + 1;
+        r[u] = (j == 0 || j == nj - 1) ? T(0) : rh[g.at(i, j, k)];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (u >= n) return;
+    const T* row = S + (long long)u * n;
+    T s = T(0);
+    for (int v = lane; v < n; v += 32) s += row[v] * r[v];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        const int j = u % nj, col = u / nj;
+        store_periodic(g, p, col % g.nx + 1, j, col / g.nx + 1, s);
+    }
 }
 
 }  // namespace ples

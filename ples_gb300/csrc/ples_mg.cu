@@ -13,6 +13,7 @@
 // mean of b net of the wall fluxes and the returned solution has zero mean.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -254,11 +255,16 @@ inline int grid1(long long n, int t = 256) {
 // ---------------------------------------------------------------------------
 struct LevelData {
     Geom g;
-    void* p = nullptr;   // inner-precision fields (T boxes)
+    int rx = 1, ry = 1, rz = 1;  // coarsening ratio from the finer level
+    int sx = 1, sy = 1, sz = 1;  // cumulative node strides relative to level 1
+    double inv_div = 1.0;        // raw metric = t * inv_div
+    double post = 1.0;           // stored coefficient = raw * post (x 1/4 on cross terms)
+    void* p = nullptr;           // inner-precision fields (T boxes)
     void* p2 = nullptr;
     void* rh = nullptr;
-    Coef<float> cf{};     // FP32 scaled coefficients (mixed)
-    Coef<double> cd{};    // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
+    void* cp = nullptr;          // LU factor c' of the eta-line operator (T box)
+    Coef<float> cf{};             // FP32 scaled coefficients (mixed)
+    Coef<double> cd{};            // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
     bool has_cf = false, has_cd = false;
 };
 
@@ -278,9 +284,11 @@ struct ples_mg_handle {
     double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
     double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes
     double* cs_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // their device buffers
+    void* coarse_S = nullptr;                            // dense inverse of the coarsest system (T)
+    int coarse_n = 0;
     int wall_passes = 3;
     double wall_q = 0.0;
-    int nu_pre = 2, nu_post = 2, nu_coarse = 40, inner_cycles = 1, smoother = 0;
+    int nu_pre = 2, nu_post = 2, nu_coarse = 40, inner_cycles = 3, smoother = 0;
     double omega = 0.8;
     std::vector<void*> allocs;
     std::string err;
@@ -316,7 +324,7 @@ int fail(ples_mg_handle* h, int code, const char* fmt, ...) {
     } while (0)
 
 // kernel kinds for the optional event timing
-enum { KIND_LINE = 0, KIND_RESTRICT = 1, KIND_PROLONG = 2, KIND_OUTER = 3, KIND_GHOST = 4, KIND_WALL = 5 };
+enum { KIND_LINE = 0, KIND_RESTRICT = 1, KIND_PROLONG = 2, KIND_OUTER = 3, KIND_COARSE = 4, KIND_WALL = 5 };
 
 void timed_begin(ples_mg_handle* h, int kind, int level) {
     if (h->timed_kind != kind || h->timed_level != level) return;
@@ -376,24 +384,24 @@ void free_tmp(std::vector<void*>& v) {
 
 // raw FP64 metric of a level into 9 temporary boxes
 int raw_metric(ples_mg_handle* h, int lev, double* gout[9], std::vector<void*>& tmp) {
-    const Geom& g = h->L[lev - 1].g;
+    const LevelData& L = h->L[lev - 1];
+    const Geom& g = L.g;
     for (int c = 0; c < 9; ++c) {
         cudaError_t e = cudaMalloc((void**)&gout[c], sizeof(double) * (size_t)g.n);
         if (e != cudaSuccess) { free_tmp(tmp); return fail(h, PLES_MG_OOM, "metric scratch: %s", cudaGetErrorString(e)); }
         tmp.push_back(gout[c]);
         CK(cudaMemsetAsync(gout[c], 0, sizeof(double) * (size_t)g.n, h->st));
     }
-    CK(launch_metric(h->xn, h->yn, h->zn, h->d.jx, h->d.jy, h->d.jz, h->d.ip, h->d.jp, h->d.kp, lev, g,
-                     gout, h->st));
+    CK(launch_metric(h->xn, h->yn, h->zn, h->d.jx, h->d.jy, h->d.jz, h->d.ip, h->d.jp, h->d.kp, L.sx, L.sy, L.sz,
+                     L.inv_div, g, gout, h->st));
     return PLES_MG_OK;
 }
 
 template <typename T>
 int scale_into(ples_mg_handle* h, int lev, double* const gr[9], Coef<T>& c) {
     const Geom& g = h->L[lev - 1].g;
-    const double ppot2 = std::ldexp(1.0, -2 * (lev - 1));
     k_scale_coef<T><<<grid1(g.n), 256, 0, h->st>>>(g.n, gr[0], gr[1], gr[2], gr[3], gr[4], gr[5], gr[6], gr[7],
-                                                   gr[8], c, ppot2);
+                                                   gr[8], c, h->L[lev - 1].post);
     CK(cudaGetLastError());
     return PLES_MG_OK;
 }
@@ -414,15 +422,7 @@ void ghost_xz(ples_mg_handle* h, const Geom& g, T* p) {
 }
 
 template <typename T>
-int line_block(const Geom& g, dim3& blk, size_t& smem) {
-    const size_t per = 2 * (size_t)(g.ny + 2) * 32 * sizeof(T);
-    int ty = (int)(72 * 1024 / per);
-    if (ty > 4) ty = 4;
-    if (ty < 1) ty = 1;
-    blk = dim3(32, ty);
-    smem = per * ty;
-    return smem <= 200 * 1024 ? 0 : -1;
-}
+size_t line_smem(const Geom& g) { return 3 * (size_t)(g.ny + 2) * 32 * sizeof(T); }
 
 // the dynamic shared-memory limit is a per-function attribute shared by all
 // handles of the process: only ever raise it
@@ -431,69 +431,88 @@ int set_smem_attrs(ples_mg_handle* h, size_t smem) {
     static size_t current = 0;
     if (smem <= current) return 0;
     current = smem;
-    CK(cudaFuncSetAttribute(k_line_relax<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_line_relax<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_dense_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
 }
 
+// nu sweeps; `zero` = the field is identically zero before the first sweep
 template <typename T>
-void smooth(ples_mg_handle* h, LevelData& L, int nu, int level) {
-    dim3 blk;
-    size_t smem;
-    line_block<T>(L.g, blk, smem);
-    Coef<T> c = coef_of<T>(L);
+void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
+    if (zero && nu == 0) cudaMemsetAsync(L.p, 0, sizeof(T) * (size_t)L.g.n, h->st);
+    const Coef<T> c = coef_of<T>(L);
     const T om = T(h->omega);
+    const size_t smem = line_smem<T>(L.g);
+    const T* cp = (const T*)L.cp;
     for (int s = 0; s < nu; ++s) {
-        if (h->smoother == 0) {
-            ghost_xz<T>(h, L.g, (T*)L.p);
-            dim3 grd((L.g.nx + 31) / 32, (L.g.nz + blk.y - 1) / blk.y);
-            timed_begin(h, KIND_LINE, level);
-            k_line_relax<T, false><<<grd, blk, smem, h->st>>>(L.g, c, (const T*)L.p, (T*)L.p2,
-                                                              (const T*)L.rh, om, 0);
-            timed_end(h, KIND_LINE, level);
-            ++h->launches;
-            std::swap(L.p, L.p2);
-        } else {
-            dim3 grd((L.g.nx / 2 + 31) / 32, (L.g.nz / 2 + blk.y - 1) / blk.y);
-            for (int colour = 0; colour < 4; ++colour) {
-                ghost_xz<T>(h, L.g, (T*)L.p);
-                timed_begin(h, KIND_LINE, level);
-                k_line_relax<T, true><<<grd, blk, smem, h->st>>>(L.g, c, (const T*)L.p, (T*)L.p,
-                                                                 (const T*)L.rh, om, colour);
-                timed_end(h, KIND_LINE, level);
-                ++h->launches;
+        const bool zin = zero && s == 0;
+        const T* pin = (const T*)L.p;
+        T* pout = (T*)L.p2;
+        timed_begin(h, KIND_LINE, level);
+        if (h->smoother == 0) {  // zebra: two launches, k parities
+            dim3 grd((L.g.nz + 1) / 2, (L.g.nx + 31) / 32);
+            if (zin) {
+                k_line_relax<T, true, true><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
+                k_line_relax<T, true, true><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
+            } else {
+                k_line_relax<T, true, false><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
+                k_line_relax<T, true, false><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
             }
+            h->launches += 2;
+        } else {  // Jacobi over lines
+            dim3 grd(L.g.nz, (L.g.nx + 31) / 32);
+            if (zin)
+                k_line_relax<T, false, true><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
+            else
+                k_line_relax<T, false, false><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
+            ++h->launches;
         }
+        timed_end(h, KIND_LINE, level);
+        std::swap(L.p, L.p2);
     }
 }
 
 template <typename T>
-void vcycle(ples_mg_handle* h) {
+void coarse_solve(ples_mg_handle* h, LevelData& C, int level) {
+    if (h->coarse_S) {
+        const int n = h->coarse_n;
+        timed_begin(h, KIND_COARSE, level);
+        k_dense_solve<T><<<(n + 7) / 8, 256, n * sizeof(T), h->st>>>(C.g, (const T*)h->coarse_S, (const T*)C.rh,
+                                                                     (T*)C.p);
+        timed_end(h, KIND_COARSE, level);
+        ++h->launches;
+    } else {
+        smooth<T>(h, C, h->nu_coarse, level, true);
+    }
+}
+
+template <typename T>
+void vcycle(ples_mg_handle* h, bool zero_fine) {
     const int nl = h->nlev;
     for (int n = 0; n < nl - 1; ++n) {
         LevelData& F = h->L[n];
         LevelData& C = h->L[n + 1];
-        smooth<T>(h, F, h->nu_pre, n + 1);
-        ghost_xz<T>(h, F.g, (T*)F.p);
+        smooth<T>(h, F, h->nu_pre, n + 1, n > 0 || zero_fine);
         dim3 blk(32, 4), grd((C.g.nx + 31) / 32, (C.g.ny + 3) / 4, C.g.nz);
         timed_begin(h, KIND_RESTRICT, n + 1);
         k_resid_restrict<T><<<grd, blk, 0, h->st>>>(F.g, C.g, coef_of<T>(F), (const T*)F.p, (const T*)F.rh,
-                                                    (T*)C.rh);
+                                                    (T*)C.rh, C.rx, C.ry, C.rz);
         timed_end(h, KIND_RESTRICT, n + 1);
         ++h->launches;
-        cudaMemsetAsync(C.p, 0, sizeof(T) * (size_t)C.g.n, h->st);
     }
-    smooth<T>(h, h->L[nl - 1], h->nu_coarse, nl);
+    coarse_solve<T>(h, h->L[nl - 1], nl);
     for (int n = nl - 2; n >= 0; --n) {
         LevelData& F = h->L[n];
         LevelData& C = h->L[n + 1];
-        ghost_xz<T>(h, C.g, (T*)C.p);
-        dim3 blk(32, 4), grd((C.g.nx + 1 + 31) / 32, (C.g.ny + 1 + 3) / 4, C.g.nz + 1);
+        dim3 blk(32, 4), grd((F.g.nx + 2 + 31) / 32, (F.g.ny + 2 + 3) / 4, F.g.nz + 2);
         timed_begin(h, KIND_PROLONG, n + 1);
-        k_prolong<T, T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p);
+        k_prolong<T, T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p, C.rx, C.ry, C.rz);
         timed_end(h, KIND_PROLONG, n + 1);
         ++h->launches;
-        smooth<T>(h, F, h->nu_post, n + 1);
+        smooth<T>(h, F, h->nu_post, n + 1, false);
     }
 }
 
@@ -524,14 +543,18 @@ int sum_interior(ples_mg_handle* h, const double* a, int squares, double* out) {
     return rc;
 }
 
+// wall ghost rows of p driven towards the fixed point of their relation
+// (Jacobi passes); the x/z ghost shell of the interior rows must already be
+// consistent, the scatter maintains it for the wall rows
 void wall_fill(ples_mg_handle* h, double* p, const double* cs3, const double* cs4, double an_dt, int passes,
                const Geom& g, const Coef<double>& c) {
-    ghost_xz<double>(h, g, p);
     dim3 blk(32, 4);
     for (int s = 0; s < passes; ++s) {
+        timed_begin(h, KIND_WALL, 1);
         k_wall_compute<<<dim3((g.nx + 31) / 32, (g.nz + 3) / 4, 2), blk, 0, h->st>>>(g, c, p, h->wbuf, cs3, cs4,
                                                                                     an_dt);
         k_wall_scatter<<<dim3((g.nx + 2 + 31) / 32, (g.nz + 2 + 3) / 4, 2), blk, 0, h->st>>>(g, p, h->wbuf);
+        timed_end(h, KIND_WALL, 1);
         h->launches += 2;
     }
 }
@@ -544,6 +567,8 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     const Geom& g = F.g;
     const double N = (double)g.nx * g.ny * g.nz;
     const double dt = h->d.dt;
+    // the caller's ghost layer is arbitrary: make the periodic shell consistent
+    ghost_xz<double>(h, g, h->x);
     // compatibility: sum(b) must equal the net wall flux (cs4 - cs3)/dt
     double sb = 0.0;
     int rc = sum_interior(h, h->b, 0, &sb);
@@ -551,7 +576,6 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     double flux = 0.0;
     if (h->cs_c[2] || h->cs_c[3]) {
         double s3 = 0.0, s4 = 0.0;
-        // wall flux sums: reuse the reduction on the compact arrays
         for (int side = 0; side < 2; ++side) {
             const double* a = h->cs_c[2 + side];
             if (!a) continue;
@@ -601,9 +625,10 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         }
         if (rel > 1e6 * rel0 && rel > 1.0) { status = PLES_MG_DIVERGED; break; }
         if (it >= max_cycles) break;
-        CK(cudaMemsetAsync(F.p, 0, sizeof(T) * (size_t)g.n, h->st));
+        // inner solve of L e = r: V-cycles from e = 0 (F.rh holds r; the
+        // residual kernel wrote it with a consistent ghost shell of zeros)
         for (int c = 0; c < h->inner_cycles; ++c) {
-            vcycle<T>(h);
+            vcycle<T>(h, c == 0);
             ++vcyc;
         }
         k_update<T><<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, (const T*)F.p);
@@ -641,9 +666,150 @@ int validate(const ples_mg_desc* d, ples_mg_handle* h) {
     if (d->nlevmax < 0 || d->nu_pre < 0 || d->nu_post < 0 || d->nu_coarse < 0 || d->inner_cycles < 0)
         return fail(h, PLES_MG_BAD_ARG, "negative level or sweep count");
     if (d->smoother != 0 && d->smoother != 1) return fail(h, PLES_MG_BAD_ARG, "unknown smoother %d", d->smoother);
+    if (d->coarsening != 0 && d->coarsening != 1)
+        return fail(h, PLES_MG_BAD_ARG, "unknown coarsening %d", d->coarsening);
     if (d->jx % 2 || d->jz % 2) return fail(h, PLES_MG_BAD_ARG, "jx and jz must be even");
+    if (d->jy > 1000) return fail(h, PLES_MG_BAD_ARG, "jy > 1000 does not fit the line smoother's shared memory");
     return PLES_MG_OK;
 }
+
+// mean node spacing along x (dir 0) or z (dir 2) over the whole grid
+double mean_spacing(const double* x, const double* y, const double* z, int jx, int jy, int jz, int dir) {
+    double s = 0.0;
+    long long n = 0;
+    const long long sj = jx + 1, sk = (long long)(jx + 1) * (jy + 1);
+    const long long step = dir == 0 ? 1 : sk;
+    for (int k = 0; k <= jz; k += (dir == 2 ? 1 : 4))
+        for (int j = 0; j <= jy; j += 4)
+            for (int i = 0; i <= jx; i += (dir == 0 ? 1 : 4)) {
+                if ((dir == 0 && i == jx) || (dir == 2 && k == jz)) continue;
+                const long long q = k * sk + j * sj + i;
+                const double dx = x[q + step] - x[q], dy = y[q + step] - y[q], dz = z[q + step] - z[q];
+                s += std::sqrt(dx * dx + dy * dy + dz * dz);
+                ++n;
+            }
+    return n ? s / n : 1.0;
+}
+
+// dense inverse of the bordered coarsest system [[M, v], [1^T, 0]] (M: the
+// level operator on interior cells and wall ghost rows, periodic in x/z;
+// v: its left null vector, +1 on interior rows and -1 on wall rows)
+template <typename T>
+int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
+    LevelData& C = h->L[lev - 1];
+    const Geom& g = C.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nj = ny + 2;
+    const int n = nx * nz * nj, m = n + 1;
+    std::vector<T> hc[9];
+    const T* src[9] = {c.a1, c.b12, c.b13, c.a2, c.b21, c.b23, c.a3, c.b31, c.b32};
+    for (int q = 0; q < 9; ++q) {
+        hc[q].resize((size_t)g.n);
+        CK(cudaMemcpyAsync(hc[q].data(), src[q], sizeof(T) * (size_t)g.n, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    auto A1 = [&](long long q) { return (double)hc[0][q]; };
+    auto B12 = [&](long long q) { return (double)hc[1][q]; };
+    auto B13 = [&](long long q) { return (double)hc[2][q]; };
+    auto A2 = [&](long long q) { return (double)hc[3][q]; };
+    auto B21 = [&](long long q) { return (double)hc[4][q]; };
+    auto B23 = [&](long long q) { return (double)hc[5][q]; };
+    auto A3 = [&](long long q) { return (double)hc[6][q]; };
+    auto B31 = [&](long long q) { return (double)hc[7][q]; };
+    auto B32 = [&](long long q) { return (double)hc[8][q]; };
+    std::vector<double> K((size_t)m * m, 0.0);
+    auto unk = [&](int i, int j, int k) {
+        i = (i - 1 + nx) % nx;
+        k = (k - 1 + nz) % nz;
+        return (k * nx + i) * nj + j;
+    };
+    for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i)
+            for (int j = 0; j < nj; ++j) {
+                const int row = unk(i, j, k);
+                double* R = &K[(size_t)row * m];
+                auto add = [&](int di, int dj, int dk, double v) { R[unk(i + di, j + dj, k + dk)] += v; };
+                if (j == 0) {  // bottom wall relation
+                    const long long q = g.at(i, 0, k);
+                    add(0, 0, 0, A2(q)); add(0, 1, 0, -A2(q));
+                    add(1, 1, 0, -B21(q)); add(1, 0, 0, -B21(q)); add(-1, 1, 0, B21(q)); add(-1, 0, 0, B21(q));
+                    add(0, 1, 1, -B23(q)); add(0, 0, 1, -B23(q)); add(0, 1, -1, B23(q)); add(0, 0, -1, B23(q));
+                    R[n] = -1.0;
+                } else if (j == nj - 1) {  // top wall relation, face ny
+                    const long long q = g.at(i, ny, k);
+                    add(0, 0, 0, A2(q)); add(0, -1, 0, -A2(q));
+                    add(1, 0, 0, B21(q)); add(1, -1, 0, B21(q)); add(-1, 0, 0, -B21(q)); add(-1, -1, 0, -B21(q));
+                    add(0, 0, 1, B23(q)); add(0, -1, 1, B23(q)); add(0, 0, -1, -B23(q)); add(0, -1, -1, -B23(q));
+                    R[n] = -1.0;
+                } else {  // interior: fdx - fsn + fsop - fsot + fav - find
+                    const long long q = g.at(i, j, k), qw = q - 1, qs = q - g.sj, qb = q - g.sk;
+                    // fdx
+                    add(1, 0, 0, A1(q)); add(0, 0, 0, -A1(q));
+                    add(1, 1, 0, B12(q)); add(0, 1, 0, B12(q)); add(1, -1, 0, -B12(q)); add(0, -1, 0, -B12(q));
+                    add(1, 0, 1, B13(q)); add(0, 0, 1, B13(q)); add(1, 0, -1, -B13(q)); add(0, 0, -1, -B13(q));
+                    // -fsn
+                    add(0, 0, 0, -A1(qw)); add(-1, 0, 0, A1(qw));
+                    add(0, 1, 0, -B12(qw)); add(-1, 1, 0, -B12(qw)); add(0, -1, 0, B12(qw)); add(-1, -1, 0, B12(qw));
+                    add(0, 0, 1, -B13(qw)); add(-1, 0, 1, -B13(qw)); add(0, 0, -1, B13(qw)); add(-1, 0, -1, B13(qw));
+                    // fsop
+                    add(0, 1, 0, A2(q)); add(0, 0, 0, -A2(q));
+                    add(1, 1, 0, B21(q)); add(1, 0, 0, B21(q)); add(-1, 1, 0, -B21(q)); add(-1, 0, 0, -B21(q));
+                    add(0, 1, 1, B23(q)); add(0, 0, 1, B23(q)); add(0, 1, -1, -B23(q)); add(0, 0, -1, -B23(q));
+                    // -fsot
+                    add(0, 0, 0, -A2(qs)); add(0, -1, 0, A2(qs));
+                    add(1, 0, 0, -B21(qs)); add(1, -1, 0, -B21(qs)); add(-1, 0, 0, B21(qs)); add(-1, -1, 0, B21(qs));
+                    add(0, 0, 1, -B23(qs)); add(0, -1, 1, -B23(qs)); add(0, 0, -1, B23(qs)); add(0, -1, -1, B23(qs));
+                    // fav
+                    add(0, 0, 1, A3(q)); add(0, 0, 0, -A3(q));
+                    add(1, 0, 1, B31(q)); add(1, 0, 0, B31(q)); add(-1, 0, 1, -B31(q)); add(-1, 0, 0, -B31(q));
+                    add(0, 1, 1, B32(q)); add(0, 1, 0, B32(q)); add(0, -1, 1, -B32(q)); add(0, -1, 0, -B32(q));
+                    // -find
+                    add(0, 0, 0, -A3(qb)); add(0, 0, -1, A3(qb));
+                    add(1, 0, 0, -B31(qb)); add(1, 0, -1, -B31(qb)); add(-1, 0, 0, B31(qb)); add(-1, 0, -1, B31(qb));
+                    add(0, 1, 0, -B32(qb)); add(0, 1, -1, -B32(qb)); add(0, -1, 0, B32(qb)); add(0, -1, -1, B32(qb));
+                    R[n] = 1.0;
+                }
+            }
+    for (int u = 0; u < n; ++u) K[(size_t)n * m + u] = 1.0;
+    // Gauss-Jordan inverse with partial pivoting
+    std::vector<double> I((size_t)m * m, 0.0);
+    for (int u = 0; u < m; ++u) I[(size_t)u * m + u] = 1.0;
+    for (int col = 0; col < m; ++col) {
+        int piv = col;
+        double best = std::fabs(K[(size_t)col * m + col]);
+        for (int r = col + 1; r < m; ++r) {
+            double v = std::fabs(K[(size_t)r * m + col]);
+            if (v > best) { best = v; piv = r; }
+        }
+        if (!(best > 0.0)) return fail(h, PLES_MG_BAD_ARG, "coarsest-level system is singular");
+        if (piv != col)
+            for (int q = 0; q < m; ++q) {
+                std::swap(K[(size_t)piv * m + q], K[(size_t)col * m + q]);
+                std::swap(I[(size_t)piv * m + q], I[(size_t)col * m + q]);
+            }
+        const double inv = 1.0 / K[(size_t)col * m + col];
+        for (int q = 0; q < m; ++q) { K[(size_t)col * m + q] *= inv; I[(size_t)col * m + q] *= inv; }
+        for (int r = 0; r < m; ++r) {
+            if (r == col) continue;
+            const double f = K[(size_t)r * m + col];
+            if (f == 0.0) continue;
+            for (int q = 0; q < m; ++q) {
+                K[(size_t)r * m + q] -= f * K[(size_t)col * m + q];
+                I[(size_t)r * m + q] -= f * I[(size_t)col * m + q];
+            }
+        }
+    }
+    std::vector<T> S((size_t)n * n);
+    for (int r = 0; r < n; ++r)
+        for (int q = 0; q < n; ++q) S[(size_t)r * n + q] = T(I[(size_t)r * m + q]);
+    int rc = dalloc(h, &h->coarse_S, sizeof(T) * (size_t)n * n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->coarse_S, S.data(), sizeof(T) * (size_t)n * n, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->coarse_n = n;
+    return PLES_MG_OK;
+}
+
+constexpr int kDenseMax = 640;  // largest coarsest system solved by the dense inverse
 
 int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     int rc = validate(d, h);
@@ -657,26 +823,13 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     CK(cudaSetDevice(h->dev));
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     h->smoother = d->smoother;
-    h->omega = d->omega > 0.0 ? d->omega : (d->smoother == 0 ? 0.8 : 1.0);
+    h->omega = d->omega > 0.0 ? d->omega : (d->smoother == 0 ? 1.3 : 0.8);
     h->nu_pre = d->nu_pre ? d->nu_pre : 2;
     h->nu_post = d->nu_post ? d->nu_post : 2;
     h->nu_coarse = d->nu_coarse ? d->nu_coarse : 40;
-    h->inner_cycles = d->inner_cycles ? d->inner_cycles : 1;
+    h->inner_cycles = d->inner_cycles ? d->inner_cycles : 5;
     const int jx = d->jx, jy = d->jy, jz = d->jz;
-    // level sizes (indy.f03 halving; the level count is limited by the grid,
-    // not by the reference's 4-level arrays, because the coarse metric reads
-    // ghost nodes on the fly)
-    int nx = jx, ny = jy, nz = jz, nl = 1;
-    h->L[0].g = make_geom(nx, ny, nz);
-    const int cap = d->nlevmax > 0 ? d->nlevmax : kMaxLev;
-    while (nl < cap && nl < kMaxLev && nx % 2 == 0 && ny % 2 == 0 && nz % 2 == 0 && nx / 2 >= 4 && ny / 2 >= 2 &&
-           nz / 2 >= 4) {
-        nx /= 2; ny /= 2; nz /= 2;
-        h->L[nl].g = make_geom(nx, ny, nz);
-        ++nl;
-    }
-    h->nlev = nl;
-    // nodes
+    // nodes (host copy needed for the spacings)
     const size_t nn = (size_t)(jx + 1) * (jy + 1) * (jz + 1);
     std::vector<double> hx, hy, hz;
     const double *sx = d->x, *sy = d->y, *sz = d->z;
@@ -691,6 +844,48 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
                     hx[q] = d->x[s]; hy[q] = d->y[s]; hz[q] = d->z[s];
                 }
         sx = hx.data(); sy = hy.data(); sz = hz.data();
+    }
+    // level sizes: the eta direction is halved every level (line smoother);
+    // full coarsening (the reference's indy.f03 / mul_met hierarchy, the
+    // default) halves x and z too, semi-coarsening halves x or z only where
+    // its spacing is within sqrt(2) of the other's.  Levels continue past the
+    // reference's four down to the dense coarsest solve.
+    const double hx1 = mean_spacing(sx, sy, sz, jx, jy, jz, 0), hz1 = mean_spacing(sx, sy, sz, jx, jy, jz, 2);
+    int nx = jx, ny = jy, nz = jz, nl = 1;
+    h->L[0].g = make_geom(nx, ny, nz);
+    const int cap = d->nlevmax > 0 ? d->nlevmax : kMaxLev;
+    while (nl < cap && nl < kMaxLev) {
+        LevelData& P = h->L[nl - 1];
+        const bool can_y = ny % 2 == 0 && ny / 2 >= 2;
+        const bool can_x = nx % 2 == 0 && nx / 2 >= 2;
+        const bool can_z = nz % 2 == 0 && nz / 2 >= 2;
+        if (!can_y) break;
+        int rx, rz;
+        if (d->coarsening == 0) {
+            if (!can_x || !can_z) break;
+            rx = rz = 2;
+        } else {
+            const double ax = hx1 * P.sx, az = hz1 * P.sz;
+            rx = (can_x && ax <= 1.4143 * az) ? 2 : 1;
+            rz = (can_z && az <= 1.4143 * ax) ? 2 : 1;
+        }
+        LevelData& C = h->L[nl];
+        C.rx = rx; C.ry = 2; C.rz = rz;
+        C.sx = P.sx * rx; C.sy = P.sy * 2; C.sz = P.sz * rz;
+        nx /= rx; ny /= 2; nz /= rz;
+        C.g = make_geom(nx, ny, nz);
+        ++nl;
+    }
+    h->nlev = nl;
+    for (int n = 0; n < nl; ++n) {
+        LevelData& L = h->L[n];
+        if (L.sx == L.sy && L.sy == L.sz) {  // mul_met's t/pot and the flux factor ppot2
+            L.inv_div = 1.0 / L.sx;
+            L.post = 1.0 / ((double)L.sx * L.sx);
+        } else {
+            L.inv_div = 1.0 / ((double)L.sx * L.sy * L.sz);
+            L.post = 1.0;
+        }
     }
     if ((rc = dalloc(h, (void**)&h->xn, nn * 8)) || (rc = dalloc(h, (void**)&h->yn, nn * 8)) ||
         (rc = dalloc(h, (void**)&h->zn, nn * 8)))
@@ -718,14 +913,27 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         free_tmp(tmp);
         const size_t es = mixed ? sizeof(float) : sizeof(double);
         if ((rc = dalloc(h, &L.p, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.p2, es * (size_t)L.g.n)) ||
-            (rc = dalloc(h, &L.rh, es * (size_t)L.g.n)))
+            (rc = dalloc(h, &L.rh, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.cp, es * (size_t)L.g.n)))
             return rc;
-        dim3 blk;
-        size_t smem;
-        if (mixed ? line_block<float>(L.g, blk, smem) : line_block<double>(L.g, blk, smem))
-            return fail(h, PLES_MG_BAD_ARG, "eta lines too long for shared memory (jy = %d)", L.g.ny);
-        if (smem > smem_max) smem_max = smem;
+        dim3 lg((L.g.nx + 127) / 128, L.g.nz);
+        if (mixed)
+            k_line_lu<float><<<lg, 128, 0, h->st>>>(L.g, L.cf, (float*)L.cp);
+        else
+            k_line_lu<double><<<lg, 128, 0, h->st>>>(L.g, L.cd, (double*)L.cp);
+        CK(cudaGetLastError());
+        size_t sm = mixed ? line_smem<float>(L.g) : line_smem<double>(L.g);
+        smem_max = std::max(smem_max, sm);
     }
+    {
+        const LevelData& C = h->L[nl - 1];
+        const int n = C.g.nx * C.g.nz * (C.g.ny + 2);
+        if (n <= kDenseMax) {
+            rc = mixed ? build_coarse_inverse<float>(h, nl, C.cf) : build_coarse_inverse<double>(h, nl, C.cd);
+            if (rc) return rc;
+            smem_max = std::max(smem_max, (size_t)n * (mixed ? 4 : 8));
+        }
+    }
+    if (smem_max > 227 * 1024) return fail(h, PLES_MG_BAD_ARG, "eta lines too long for shared memory");
     if ((rc = mixed ? set_smem_attrs<float>(h, smem_max) : set_smem_attrs<double>(h, smem_max))) return rc;
     const Geom& g = h->L[0].g;
     if ((rc = dalloc(h, (void**)&h->x, 8 * (size_t)g.n)) || (rc = dalloc(h, (void**)&h->b, 8 * (size_t)g.n)) ||
@@ -1075,6 +1283,7 @@ int ples_mg_apply_ghost_fill(ples_mg_handle* h, int level, double* pr, const dou
             c4 = h->cs_c[3];
         }
         // the handle's wall buffer is sized for level 1 and serves every level
+        ghost_xz<double>(h, g, P);
         wall_fill(h, P, c3, c4, level == 1 ? 1.0 / h->d.dt : 0.0, passes, g, c);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) { free_tmp(tmp); return fail(h, PLES_MG_CUDA_ERROR, "ghost fill: %s", cudaGetErrorString(e)); }
@@ -1098,7 +1307,9 @@ int ples_mg_apply_restrict(ples_mg_handle* h, int level, const double* rh, doubl
             free_tmp(tmp);
             return rc;
         }
-        k_restrict<double><<<dim3((gc.nx + 31) / 32, (gc.ny + 3) / 4, gc.nz), dim3(32, 4), 0, h->st>>>(gf, gc, F, C);
+        const LevelData& LC = h->L[level];
+        k_restrict<double><<<dim3((gc.nx + 31) / 32, (gc.ny + 3) / 4, gc.nz), dim3(32, 4), 0, h->st>>>(
+            gf, gc, F, C, LC.rx, LC.ry, LC.rz);
         rc = get_box(h, gc, 0, C, out, tmp);
         free_tmp(tmp);
         return rc;
@@ -1119,8 +1330,9 @@ int ples_mg_apply_prolong(ples_mg_handle* h, int level, double* prf, const doubl
             free_tmp(tmp);
             return rc;
         }
-        k_prolong<double, double><<<dim3((gc.nx + 1 + 31) / 32, (gc.ny + 1 + 3) / 4, gc.nz + 1), dim3(32, 4), 0,
-                                    h->st>>>(gf, gc, F, C);
+        const LevelData& LC = h->L[level];
+        k_prolong<double, double><<<dim3((gf.nx + 2 + 31) / 32, (gf.ny + 2 + 3) / 4, gf.nz + 2), dim3(32, 4), 0,
+                                    h->st>>>(gf, gc, F, C, LC.rx, LC.ry, LC.rz);
         rc = get_box(h, gf, 1, F, prf, tmp);
         free_tmp(tmp);
         return rc;

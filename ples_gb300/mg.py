@@ -40,7 +40,7 @@ class Desc(C.Structure):
                 ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
                 ("z", C.POINTER(C.c_double)), ("dt", C.c_double), ("device", C.c_int),
                 ("nu_pre", C.c_int), ("nu_post", C.c_int), ("nu_coarse", C.c_int),
-                ("inner_cycles", C.c_int), ("smoother", C.c_int)]
+                ("inner_cycles", C.c_int), ("smoother", C.c_int), ("coarsening", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -115,7 +115,7 @@ class Multigrid:
 
     def __init__(self, x, y, z, ip=0, jp=1, kp=0, precision="mixed", dt=1.0, device=0,
                  nlevmax=0, omega=0.0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0,
-                 smoother=0, coords_layout=COORDS_NODES, jx=None, jy=None, jz=None):
+                 smoother=0, coarsening=0, coords_layout=COORDS_NODES):
         self._L = load()
         self._x, self._y, self._z = _f64(x), _f64(y), _f64(z)
         if coords_layout == COORDS_NODES:
@@ -133,7 +133,7 @@ class Multigrid:
         d.z = self._z.ctypes.data_as(dp)
         d.dt, d.device = dt, device
         d.nu_pre, d.nu_post, d.nu_coarse = nu_pre, nu_post, nu_coarse
-        d.inner_cycles, d.smoother = inner_cycles, smoother
+        d.inner_cycles, d.smoother, d.coarsening = inner_cycles, smoother, coarsening
         h = C.c_void_p()
         rc = self._L.ples_mg_create(C.byref(d), C.byref(h))
         if rc != OK:

@@ -45,8 +45,16 @@ def case0():
 
 
 @pytest.fixture(scope="module")
-def dev_mixed(case0):
+def dev_full(case0):
+    """The reference's full-coarsening hierarchy (mul_met levels)."""
     with mg.Multigrid(case0["x"], case0["y"], case0["z"], precision="mixed") as m:
+        yield m
+
+
+@pytest.fixture(scope="module")
+def dev_mixed(case0):
+    """Semi-coarsened hierarchy with the Jacobi line smoother."""
+    with mg.Multigrid(case0["x"], case0["y"], case0["z"], precision="mixed", coarsening=1, smoother=1) as m:
         yield m
 
 
@@ -57,9 +65,9 @@ def dev_fp64(case0):
 
 
 @pytest.mark.parametrize("level", [1, 2, 3, 4])
-def test_metric_bit_exact(case0, dev_mixed, level):
+def test_metric_bit_exact(case0, dev_full, level):
     for name in mg.METRIC_NAMES:
-        a = dev_mixed.metric(level, name)
+        a = dev_full.metric(level, name)
         b = case0["orc"].metric(level, name)
         assert a.shape == b.shape
         assert np.array_equal(a, b), (name, np.abs(a - b).max())
@@ -84,22 +92,22 @@ def test_metric_sample_deck_and_ghosted_layout():
 
 
 @pytest.mark.parametrize("level", [1, 2, 3])
-def test_residual_fp64_and_fp32(case0, dev_mixed, level):
+def test_residual_fp64_and_fp32(case0, dev_full, level):
     orc = case0["orc"]
     nx, ny, nz = orc.dims(level)
     rng = np.random.default_rng(level)
     pr = np.asfortranarray(rng.standard_normal((nx + 2, ny + 2, nz + 2)))
     rh = np.asfortranarray(rng.standard_normal((nx, ny, nz)))
     ref = orc.resid(level, pr, rh)
-    r64 = dev_mixed.residual(level, pr, rh, "fp64")
+    r64 = dev_full.residual(level, pr, rh, "fp64")
     assert np.abs(r64 - ref).max() <= 1e-12 * np.abs(ref).max()
-    r32 = dev_mixed.residual(level, pr, rh, "fp32")
+    r32 = dev_full.residual(level, pr, rh, "fp32")
     scale = np.abs(orc.resid(level, pr, np.zeros_like(rh))).max() + np.abs(rh).max()
     assert np.abs(r32 - ref).max() <= 2e-5 * scale
 
 
 @pytest.mark.parametrize("level", [1, 2])
-def test_ghost_fill_fixed_point(case0, dev_mixed, level):
+def test_ghost_fill_fixed_point(case0, dev_full, level):
     orc = case0["orc"]
     nx, ny, nz = orc.dims(level)
     rng = np.random.default_rng(10 + level)
@@ -110,29 +118,47 @@ def test_ghost_fill_fixed_point(case0, dev_mixed, level):
     ref = pr.copy(order="F")
     for _ in range(12):
         ref = orc.ghost_fill(level, ref, cs=cs)
-    out = dev_mixed.ghost_fill(level, pr, cs=cs, passes=60)
+    out = dev_full.ghost_fill(level, pr, cs=cs, passes=60)
     np.testing.assert_array_equal(out[1:-1, 1:-1, 1:-1], pr[1:-1, 1:-1, 1:-1])
     assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
-def test_restriction_and_prolongation(case0, dev_mixed):
+def test_restriction_and_prolongation(case0, dev_full):
     orc = case0["orc"]
     rng = np.random.default_rng(4)
     for level in (1, 2, 3):
         nx, ny, nz = orc.dims(level)
         r = np.asfortranarray(rng.standard_normal((nx, ny, nz)))
-        assert np.array_equal(dev_mixed.restrict(level, r), orc.restrict(level, r))
+        assert np.array_equal(dev_full.restrict(level, r), orc.restrict(level, r))
         cx, cy, cz = orc.dims(level + 1)
         pf = np.asfortranarray(rng.standard_normal((nx + 2, ny + 2, nz + 2)))
         pc = np.asfortranarray(rng.standard_normal((cx + 2, cy + 2, cz + 2)))
-        a = dev_mixed.prolong(level, pf, pc)
+        a = dev_full.prolong(level, pf, pc)
         b = orc.prolong(level, pf, pc)
         assert np.abs(a - b).max() <= 1e-14 * np.abs(b).max()
 
 
-@pytest.mark.parametrize("prec", ["mixed", "fp64"])
-def test_solve_parity(case0, dev_mixed, dev_fp64, prec):
-    m = dev_mixed if prec == "mixed" else dev_fp64
+def test_semi_coarsened_transfers(dev_mixed):
+    """Automatic coarsening keeps x where the grid is anisotropic (64x32x64
+    with dx = 2 dz -> 64x16x32): restriction preserves sums (x -1/#children),
+    prolongation reproduces constants on every fine cell, ghosts included."""
+    assert dev_mixed.dims(2) == (64, 16, 32)
+    rng = np.random.default_rng(8)
+    for level in range(1, dev_mixed.nlevel):
+        nx, ny, nz = dev_mixed.dims(level)
+        cx, cy, cz = dev_mixed.dims(level + 1)
+        ratio = (nx // cx) * (ny // cy) * (nz // cz)
+        r = np.asfortranarray(rng.standard_normal((nx, ny, nz)))
+        rc = dev_mixed.restrict(level, r)
+        np.testing.assert_allclose(rc.sum(), -r.sum() / ratio, atol=1e-11 * np.abs(r).sum())
+        out = dev_mixed.prolong(level, np.zeros((nx + 2, ny + 2, nz + 2), order="F"),
+                                np.full((cx + 2, cy + 2, cz + 2), 1.5, order="F"))
+        np.testing.assert_allclose(out, 1.5, rtol=1e-15)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64", "full"])
+def test_solve_parity(case0, dev_mixed, dev_fp64, dev_full, prec):
+    m = {"mixed": dev_mixed, "fp64": dev_fp64, "full": dev_full}[prec]
     fi, st = m.solve(case0["rhs"], rel_tol=REL_TOL, max_cycles=100)
     assert st["status"] == mg.OK and st["rel_residual"] <= REL_TOL
     l2, mx = _rel(_zm(fi), case0["ref"])
@@ -181,7 +207,7 @@ def test_multi_reference_semantics(case0, dev_mixed):
     assert st["status"] == mg.NOT_CONVERGED and st["outer_iterations"] == 2
 
 
-def test_zebra_smoother_same_solution(case0):
+def test_jacobi_smoother_same_solution(case0):
     with mg.Multigrid(case0["x"], case0["y"], case0["z"], smoother=1) as m:
         fi, st = m.solve(case0["rhs"], rel_tol=REL_TOL)
     assert st["status"] == mg.OK
