@@ -1,0 +1,128 @@
+!***********************************************************************
+! ples_mg_iface -- iso_c_binding interface of the GB300 pressure multigrid
+! (include/ples_mg.h) and the two calls that replace PLES's CPU solver:
+!
+!   ples_mg_setup : after metrica (fsrc/stratiParticle.f03:767), in place of
+!                   mul_met / wall (:768-769); builds the coefficient
+!                   hierarchy on the GPU from the node coordinates x,y,z
+!                   (myarrays_metri3, single-domain extent -8:n1+8, ...).
+!   multi_gpu     : drop-in body for multi (fsrc/multigrid.f03:42-653) at
+!                   the call site fsrc/stratiParticle.f03:2881-2887: same
+!                   eps (absolute max-norm stop) and ficycle meaning; fi
+!                   (myarrays_velo3, 0:n1+1,0:n2+1,0:n3+1 on one rank) is
+!                   overwritten with the solution including its ghost layer.
+!
+! Not compiled in this repository's build (no Fortran compiler is assumed);
+! a PLES build adds it to its object list and links libples_mg.so.
+!***********************************************************************
+module ples_mg_iface
+    use iso_c_binding
+    implicit none
+
+    integer(c_int), parameter :: PLES_MG_OK = 0, PLES_MG_NOT_CONVERGED = 1
+    integer(c_int), parameter :: PLES_MG_PREC_FP64 = 0, PLES_MG_PREC_MIXED = 1
+    integer(c_int), parameter :: PLES_MG_COORDS_NODES = 0, PLES_MG_COORDS_GHOSTED8 = 1
+
+    type, bind(C) :: ples_mg_desc
+        integer(c_int) :: jx, jy, jz
+        integer(c_int) :: ip, jp, kp
+        integer(c_int) :: nlevmax
+        real(c_double) :: omega
+        integer(c_int) :: precision
+        integer(c_int) :: coords_layout
+        type(c_ptr)    :: x, y, z
+        real(c_double) :: dt
+        integer(c_int) :: device
+        integer(c_int) :: nu_pre, nu_post
+        integer(c_int) :: nu_coarse
+        integer(c_int) :: inner_cycles
+        integer(c_int) :: smoother
+        integer(c_int) :: coarsening
+    end type ples_mg_desc
+
+    type, bind(C) :: ples_mg_stats
+        integer(c_int) :: outer_iterations
+        integer(c_int) :: vcycles
+        real(c_double) :: rel_residual
+        real(c_double) :: max_residual
+        real(c_double) :: rhs_norm
+        real(c_double) :: rhs_mean_removed
+        real(c_double) :: seconds
+        integer(c_int) :: status
+    end type ples_mg_stats
+
+    interface
+        integer(c_int) function ples_mg_create(desc, handle) bind(C, name="ples_mg_create")
+            import :: ples_mg_desc, c_int, c_ptr
+            type(ples_mg_desc), intent(in) :: desc
+            type(c_ptr), intent(out) :: handle
+        end function ples_mg_create
+
+        integer(c_int) function ples_mg_solve(handle, fi, rhs, cs, rel_tol, abs_tol_max, &
+                                              max_cycles, stats) bind(C, name="ples_mg_solve")
+            import :: c_int, c_ptr, c_double, ples_mg_stats
+            type(c_ptr), value :: handle, fi, rhs, cs
+            real(c_double), value :: rel_tol, abs_tol_max
+            integer(c_int), value :: max_cycles
+            type(ples_mg_stats), intent(out) :: stats
+        end function ples_mg_solve
+
+        subroutine ples_mg_destroy(handle) bind(C, name="ples_mg_destroy")
+            import :: c_ptr
+            type(c_ptr), value :: handle
+        end subroutine ples_mg_destroy
+
+        function ples_mg_strerror(code) bind(C, name="ples_mg_strerror")
+            import :: c_int, c_ptr
+            integer(c_int), value :: code
+            type(c_ptr) :: ples_mg_strerror
+        end function ples_mg_strerror
+    end interface
+
+    type(c_ptr), save :: mg_handle = c_null_ptr
+
+contains
+
+    !-------------------------------------------------------------------
+    ! after metrica: x, y, z are the ghosted node arrays of myarrays_metri3
+    ! (one rank holds the whole domain); only planes -8..jz+8 are read.
+    subroutine ples_mg_setup(x, y, z, jx, jy, jz, ip, jp, kp, dt, precision)
+        real(c_double), target, intent(in) :: x(-8:, -8:, -8:), y(-8:, -8:, -8:), z(-8:, -8:, -8:)
+        integer, intent(in) :: jx, jy, jz, ip, jp, kp, precision
+        real(c_double), intent(in) :: dt
+        type(ples_mg_desc) :: d
+        integer(c_int) :: stat
+
+        if (size(x, 1) /= jx + 17 .or. size(x, 2) /= jy + 17) error stop 'ples_mg_setup: x extents'
+        d = ples_mg_desc(jx=jx, jy=jy, jz=jz, ip=ip, jp=jp, kp=kp, nlevmax=0, omega=0.d0, &
+                         precision=precision, coords_layout=PLES_MG_COORDS_GHOSTED8, &
+                         x=c_loc(x(-8, -8, -8)), y=c_loc(y(-8, -8, -8)), z=c_loc(z(-8, -8, -8)), &
+                         dt=dt, device=0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0, &
+                         smoother=0, coarsening=0)
+        if (c_associated(mg_handle)) call ples_mg_destroy(mg_handle)
+        stat = ples_mg_create(d, mg_handle)
+        if (stat /= PLES_MG_OK) error stop 'ples_mg_create failed'
+    end subroutine ples_mg_setup
+
+    !-------------------------------------------------------------------
+    ! replacement of multi: eps and ficycle as in Agenerale.in; returns the
+    ! number of cycles in ktime like the reference's loop counter
+    subroutine multi_gpu(eps, ficycle, fi, rhs, cs1, cs2, cs3, cs4, cs5, cs6, ktime)
+        real(c_double), intent(in) :: eps
+        integer, intent(in) :: ficycle
+        real(c_double), target, intent(inout) :: fi(0:, 0:, 0:)
+        real(c_double), target, intent(in) :: rhs(:, :, :)
+        real(c_double), target, intent(in) :: cs1(:, :), cs2(:, :), cs3(:, :), cs4(:, :), cs5(:, :), cs6(:, :)
+        integer, intent(out) :: ktime
+        type(c_ptr), target :: cs(6)
+        type(ples_mg_stats) :: st
+        integer(c_int) :: stat
+
+        cs = [c_loc(cs1), c_loc(cs2), c_loc(cs3), c_loc(cs4), c_loc(cs5), c_loc(cs6)]
+        stat = ples_mg_solve(mg_handle, c_loc(fi), c_loc(rhs), c_loc(cs), 0.d0, eps, &
+                             int(ficycle, c_int), st)
+        if (stat /= PLES_MG_OK .and. stat /= PLES_MG_NOT_CONVERGED) error stop 'ples_mg_solve failed'
+        ktime = st%outer_iterations
+    end subroutine multi_gpu
+
+end module ples_mg_iface
