@@ -64,6 +64,12 @@ struct Coef {
 template <typename T>
 __device__ __forceinline__ T ld(const T* p, long long q) { return __ldg(p + q); }
 
+// hint the L2 to fetch the line holding p[q] (no register, no L1 allocation)
+template <typename T>
+__device__ __forceinline__ void pf_l2(const T* p, long long q) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + q));
+}
+
 // Store v at interior cell (i,j,k) and at its periodic images in the x/z
 // ghost shell (the reference's periodic copies, corner lines, vertical frame
 // and horizontal square, multigrid.f03:1145-1158, 1325-1620).
@@ -313,6 +319,16 @@ __global__ void __launch_bounds__(256) k_line_relax(Geom g, Coef<T> c, const T* 
     if (act) {
         for (int j = w; j < nj; j += nw) {
             const long long q = g.at(i, j, k);
+            if (j + nw < nj) {  // next row of this warp: start its lines towards L2
+                const long long qn = q + nw * sj;
+                pf_l2(c.a1, qn); pf_l2(c.b12, qn); pf_l2(c.b13, qn);
+                pf_l2(c.a2, qn); pf_l2(c.b21, qn); pf_l2(c.b23, qn);
+                pf_l2(c.a3, qn); pf_l2(c.b31, qn); pf_l2(c.b32, qn);
+                pf_l2(c.a3, qn - sk); pf_l2(c.b31, qn - sk); pf_l2(c.b32, qn - sk);
+                pf_l2(rh, qn); pf_l2(cpa, qn);
+                if (!ZIN) pf_l2(pin, qn + sj);
+                if (!zk) { pf_l2(pk, qn + sj + sk); pf_l2(pk, qn + sj - sk); }
+            }
             T f, a, im;
             if (j == 0) {
                 const T a2 = ld(c.a2, q);
@@ -509,6 +525,41 @@ __global__ void k_prolong(Geom gf, Geom gc, Tf* __restrict__ pf, const Tc* __res
             for (int a = 0; a < ni; ++a) s += wi[a] * wj[b] * wk[c] * pc[gc.at(ci[a], cj[b], ck[c])];
     const long long q = gf.at(fi, fj, fk);
     pf[q] = pf[q] + Tf(s);
+}
+
+// Prolongation for a level coarsened in x (rx = 2): one thread makes the
+// two fine cells 2c and 2c+1, which interpolate the same coarse pair
+// (c, c+1) with weights (3/4, 1/4) and (1/4, 3/4); y and z as in k_prolong.
+template <typename T>
+__global__ void k_prolong_x2(Geom gf, Geom gc, T* __restrict__ pf, const T* __restrict__ pc, int ry, int rz) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int fj = blockIdx.y * blockDim.y + threadIdx.y;
+    const int fk = blockIdx.z;
+    if (c > gc.nx || fj > gf.ny + 1) return;
+    const int cj = ry == 2 ? fj >> 1 : fj, ck = rz == 2 ? fk >> 1 : fk;
+    const T wj0 = ry == 2 ? ((fj & 1) ? T(0.25) : T(0.75)) : T(1);
+    const T wk0 = rz == 2 ? ((fk & 1) ? T(0.25) : T(0.75)) : T(1);
+    const long long q = gc.at(c, cj, ck);
+    const int oj = (int)gc.sj, ok = (int)gc.sk;
+    T a = wj0 * wk0 * pc[q], bb = wj0 * wk0 * pc[q + 1];
+    if (ry == 2) {
+        const T w = (T(1) - wj0) * wk0;
+        a += w * pc[q + oj];
+        bb += w * pc[q + oj + 1];
+    }
+    if (rz == 2) {
+        const T w = wj0 * (T(1) - wk0);
+        a += w * pc[q + ok];
+        bb += w * pc[q + ok + 1];
+        if (ry == 2) {
+            const T w2 = (T(1) - wj0) * (T(1) - wk0);
+            a += w2 * pc[q + oj + ok];
+            bb += w2 * pc[q + oj + ok + 1];
+        }
+    }
+    const long long qf = gf.at(2 * c, fj, fk);
+    pf[qf] = pf[qf] + (T(0.75) * a + T(0.25) * bb);
+    pf[qf + 1] = pf[qf + 1] + (T(0.25) * a + T(0.75) * bb);
 }
 
 // ---------------------------------------------------------------------------

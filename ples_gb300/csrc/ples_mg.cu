@@ -98,6 +98,72 @@ __global__ void k_resid_outer(Geom g, Coef<double> c, const double* __restrict__
     }
 }
 
+// Face fluxes of the 19-point operator with the scaled coefficients (the
+// bracketed terms of res_dx / res_sop / res_av, resid_sndrcv.f03:85-147):
+// flux through csi-face i, eta-face j, zeta-face k of cell (i,j,k).
+__device__ __forceinline__ double flux_x(const Geom& g, const Coef<double>& c, const double* __restrict__ p,
+                                         long long q) {
+    const long long sj = g.sj, sk = g.sk;
+    return c.a1[q] * (p[q + 1] - p[q]) + c.b12[q] * (p[q + 1 + sj] + p[q + sj] - p[q + 1 - sj] - p[q - sj]) +
+           c.b13[q] * (p[q + 1 + sk] + p[q + sk] - p[q + 1 - sk] - p[q - sk]);
+}
+__device__ __forceinline__ double flux_y(const Geom& g, const Coef<double>& c, const double* __restrict__ p,
+                                         long long q) {
+    const long long sj = g.sj, sk = g.sk;
+    return c.a2[q] * (p[q + sj] - p[q]) + c.b21[q] * (p[q + 1 + sj] + p[q + 1] - p[q - 1 + sj] - p[q - 1]) +
+           c.b23[q] * (p[q + sj + sk] + p[q + sk] - p[q + sj - sk] - p[q - sk]);
+}
+__device__ __forceinline__ double flux_z(const Geom& g, const Coef<double>& c, const double* __restrict__ p,
+                                         long long q) {
+    const long long sj = g.sj, sk = g.sk;
+    return c.a3[q] * (p[q + sk] - p[q]) + c.b31[q] * (p[q + 1 + sk] + p[q + 1] - p[q - 1 + sk] - p[q - 1]) +
+           c.b32[q] * (p[q + sj + sk] + p[q + sj] - p[q - sj + sk] - p[q - sj]);
+}
+
+// r = b - L(x) with every face flux evaluated once and shared by its two
+// cells: the csi-face flux through the lane shuffle, the eta-face flux
+// through shared memory, the zeta-face flux carried while the thread walks
+// KC planes in k.  The FP64 pipe is the bound of this kernel, so sharing
+// roughly halves its time.  Per-block partial sum of squares and max |r|.
+template <typename Ti, int KC>
+__global__ void __launch_bounds__(256) k_resid_outer2(Geom g, Coef<double> c, const double* __restrict__ x,
+                                                      const double* __restrict__ b, Ti* __restrict__ rin,
+                                                      double* __restrict__ psq, double* __restrict__ pmax) {
+    __shared__ double sN[8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + tx + 1, j = blockIdx.y * 8 + ty + 1;
+    const int k0 = blockIdx.z * KC + 1, k1 = min(k0 + KC - 1, g.nz);
+    const bool act = i <= g.nx && j <= g.ny;
+    const int ic = min(i, g.nx), jc = min(j, g.ny);  // keep idle threads' loads in the box
+    double s = 0.0, m = 0.0;
+    double fB = flux_z(g, c, x, g.at(ic, jc, k0 - 1));
+    for (int k = k0; k <= k1; ++k) {
+        const long long q = g.at(ic, jc, k);
+        const double fE = flux_x(g, c, x, q);
+        double fW = __shfl_up_sync(0xffffffffu, fE, 1);
+        if (tx == 0) fW = flux_x(g, c, x, q - 1);
+        const double fN = flux_y(g, c, x, q);
+        sN[ty][tx] = fN;
+        __syncthreads();
+        const double fS = ty > 0 ? sN[ty - 1][tx] : flux_y(g, c, x, q - g.sj);
+        __syncthreads();
+        const double fF = flux_z(g, c, x, q);
+        if (act) {
+            const double r = b[q] - ((fE - fW) + (fN - fS) + (fF - fB));
+            rin[q] = Ti(r);
+            s += r * r;
+            m = fmax(m, fabs(r));
+        }
+        fB = fF;
+    }
+    block_reduce_sum_max(s, m);
+    if (threadIdx.x == 0) {
+        const long long blk = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        psq[blk] = s;
+        pmax[blk] = m;
+    }
+}
+
 // sum / sum of squares of interior cells, per-block partials
 __global__ void k_sum_interior(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum) {
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -507,9 +573,14 @@ void vcycle(ples_mg_handle* h, bool zero_fine) {
     for (int n = nl - 2; n >= 0; --n) {
         LevelData& F = h->L[n];
         LevelData& C = h->L[n + 1];
-        dim3 blk(32, 4), grd((F.g.nx + 2 + 31) / 32, (F.g.ny + 2 + 3) / 4, F.g.nz + 2);
         timed_begin(h, KIND_PROLONG, n + 1);
-        k_prolong<T, T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p, C.rx, C.ry, C.rz);
+        if (C.rx == 2) {
+            dim3 blk(32, 4), grd((C.g.nx + 1 + 31) / 32, (F.g.ny + 2 + 3) / 4, F.g.nz + 2);
+            k_prolong_x2<T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p, C.ry, C.rz);
+        } else {
+            dim3 blk(32, 4), grd((F.g.nx + 2 + 31) / 32, (F.g.ny + 2 + 3) / 4, F.g.nz + 2);
+            k_prolong<T, T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p, C.rx, C.ry, C.rz);
+        }
         timed_end(h, KIND_PROLONG, n + 1);
         ++h->launches;
         smooth<T>(h, F, h->nu_post, n + 1, false);
@@ -601,14 +672,15 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     st->rhs_norm = std::sqrt(bn2);
     st->rhs_mean_removed = shift;
 
-    const dim3 rg = red_grid(g);
+    constexpr int kKC = 8;
+    const dim3 rg((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kKC - 1) / kKC);
     const long long nblk = (long long)rg.x * rg.y * rg.z;
     double rel = 0.0, rmax = 0.0, rel0 = -1.0;
     int it = 0, status = PLES_MG_NOT_CONVERGED, vcyc = 0;
     for (;;) {
         wall_fill(h, h->x, h->cs_c[2], h->cs_c[3], 1.0 / dt, h->wall_passes, g, F.cd);
         timed_begin(h, KIND_OUTER, 1);
-        k_resid_outer<T><<<rg, kRedThreads, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b);
+        k_resid_outer2<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b);
         timed_end(h, KIND_OUTER, 1);
         ++h->launches;
         CK(cudaGetLastError());
@@ -1331,8 +1403,12 @@ int ples_mg_apply_prolong(ples_mg_handle* h, int level, double* prf, const doubl
             return rc;
         }
         const LevelData& LC = h->L[level];
-        k_prolong<double, double><<<dim3((gf.nx + 2 + 31) / 32, (gf.ny + 2 + 3) / 4, gf.nz + 2), dim3(32, 4), 0,
-                                    h->st>>>(gf, gc, F, C, LC.rx, LC.ry, LC.rz);
+        if (LC.rx == 2)
+            k_prolong_x2<double><<<dim3((gc.nx + 1 + 31) / 32, (gf.ny + 2 + 3) / 4, gf.nz + 2), dim3(32, 4), 0,
+                                   h->st>>>(gf, gc, F, C, LC.ry, LC.rz);
+        else
+            k_prolong<double, double><<<dim3((gf.nx + 2 + 31) / 32, (gf.ny + 2 + 3) / 4, gf.nz + 2), dim3(32, 4),
+                                        0, h->st>>>(gf, gc, F, C, LC.rx, LC.ry, LC.rz);
         rc = get_box(h, gf, 1, F, prf, tmp);
         free_tmp(tmp);
         return rc;
