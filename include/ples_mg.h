@@ -149,6 +149,30 @@ int ples_mg_counters(ples_mg_handle *h, long long *launches, long long *device_b
 int ples_mg_kernel_timing(ples_mg_handle *h, int kind, int level);
 int ples_mg_kernel_time(ples_mg_handle *h, double *total_ms, long long *launches);
 
+/* ---- fine-level residual norms without device allocation -------------
+ * No counterpart in the reference: it has no device and no allocator to
+ * avoid.  For callers that must not allocate device memory during the call
+ * (a time-step loop whose fields fill the card, an allocator-free section):
+ * it calls no cudaMalloc/cudaFree and no allocating library routine, and
+ * works in a fixed scratch array inside the library (1 MiB + 16 B per
+ * device).  Grids needing more than 65536 blocks of 32 x 8 x 8 cells (about
+ * 512^3 cells) are rejected with PLES_MG_BAD_ARG.
+ *
+ * On the fine level: r = L(fi) - rhs as in ples_mg_apply_residual with
+ * level 1 and FP64 (resid_sndrcv.f03:2-156), and norms[0] = sum of r^2,
+ * norms[1] = max |r| (the stop test of multi, multigrid.f03:595-631).
+ * d_fi (0:jx+1,0:jy+1,0:jz+1) and d_rhs (1:jx,1:jy,1:jz) are device
+ * buffers; the ghost layer of d_fi is used as given.  d_r (1:jx,1:jy,1:jz,
+ * device) receives r, or is NULL.  norms is host memory; the call returns
+ * after the result reached it.  stream NULL = the handle's stream.
+ * The first call on each device looks the scratch address up
+ * (cudaGetSymbolAddress, which may load the module), so make that first call
+ * before any stream capture.  All calls on one device share the scratch:
+ * calls that overlap in time on that device race; serialise them. */
+int ples_mg_residual_norms_device(ples_mg_handle *h, const double *d_fi,
+                                  const double *d_rhs, double *d_r, void *stream,
+                                  double norms[2]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1440,3 +1441,152 @@ int ples_mg_kernel_time(ples_mg_handle* h, double* total_ms, long long* launches
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Fine-level residual norms without device allocation.
+//
+// ples_mg_residual_norms_device is for callers that must not allocate device
+// memory while they run: a time-step loop whose flow fields already fill the
+// card, or code that holds the device in an allocator-free section, where a
+// cudaMalloc may fail and where the device-wide synchronisation of cudaFree
+// would stall work on other streams.  The operator entry points above
+// allocate temporaries per call; this one works in a fixed scratch array
+// compiled into the library instead.
+//
+// The scratch holds kNormMaxBlocks per-block partial pairs (sum of squares,
+// max |r|) plus the two final values: 2 * 65536 + 2 doubles, 1 MiB + 16 B per
+// device.  One block covers 32 x 8 cells of 8 planes, so grids up to about
+// 512^3 cells fit; a larger grid is rejected with PLES_MG_BAD_ARG.  Nothing in
+// the scratch needs to start at zero: each call overwrites every partial it
+// reads and then the two final values.  Every call on a device shares the
+// same array, so calls that overlap in time on that device (two host threads,
+// or two streams whose work interleaves) race on it; serialise them.
+namespace {
+
+constexpr int kNormMaxBlocks = 65536;
+constexpr int kNormKC = 8;
+constexpr int kNormMaxDevices = 64;
+static __device__ __align__(256) double g_norm_scratch[2 * kNormMaxBlocks + 2];
+
+// the caller's fi (0:jx+1,0:jy+1,0:jz+1), column-major
+struct CompactP {
+    const double* p;
+    long long sj, sk;
+};
+
+// face fluxes of flux_x/y/z with the pressure read at qp of the caller's fi
+__device__ __forceinline__ double cflux_x(const Coef<double>& c, long long q, const CompactP& P, long long qp) {
+    const double* p = P.p;
+    const long long sj = P.sj, sk = P.sk;
+    return c.a1[q] * (p[qp + 1] - p[qp]) + c.b12[q] * (p[qp + 1 + sj] + p[qp + sj] - p[qp + 1 - sj] - p[qp - sj]) +
+           c.b13[q] * (p[qp + 1 + sk] + p[qp + sk] - p[qp + 1 - sk] - p[qp - sk]);
+}
+__device__ __forceinline__ double cflux_y(const Coef<double>& c, long long q, const CompactP& P, long long qp) {
+    const double* p = P.p;
+    const long long sj = P.sj, sk = P.sk;
+    return c.a2[q] * (p[qp + sj] - p[qp]) + c.b21[q] * (p[qp + 1 + sj] + p[qp + 1] - p[qp - 1 + sj] - p[qp - 1]) +
+           c.b23[q] * (p[qp + sj + sk] + p[qp + sk] - p[qp + sj - sk] - p[qp - sk]);
+}
+__device__ __forceinline__ double cflux_z(const Coef<double>& c, long long q, const CompactP& P, long long qp) {
+    const double* p = P.p;
+    const long long sj = P.sj, sk = P.sk;
+    return c.a3[q] * (p[qp + sk] - p[qp]) + c.b31[q] * (p[qp + 1 + sk] + p[qp + 1] - p[qp - 1 + sk] - p[qp - 1]) +
+           c.b32[q] * (p[qp + sj + sk] + p[qp + sj] - p[qp - sj + sk] - p[qp - sj]);
+}
+
+// r = L(fi) - rhs (the sign of resid_sndrcv.f03:2-156) on the fine level,
+// read straight from the caller's arrays, with the flux sharing of
+// k_resid_outer2; optional r output in the (1:jx,1:jy,1:jz) layout and
+// per-block partials into part[blk] (sum of squares), part[maxoff + blk]
+// (max |r|).  The ghost layer of fi is used as the caller left it.
+template <int KC>
+__global__ void __launch_bounds__(256) k_resid_norm_compact(Geom g, Coef<double> c, CompactP P,
+                                                            const double* __restrict__ rhs,
+                                                            double* __restrict__ rout, double* __restrict__ part,
+                                                            long long maxoff) {
+    __shared__ double sN[8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + tx + 1, j = blockIdx.y * 8 + ty + 1;
+    const int k0 = blockIdx.z * KC + 1, k1 = min(k0 + KC - 1, g.nz);
+    const bool act = i <= g.nx && j <= g.ny;
+    const int ic = min(i, g.nx), jc = min(j, g.ny);
+    const long long qp0 = ic + P.sj * jc;
+    double s = 0.0, m = 0.0;
+    double fB = cflux_z(c, g.at(ic, jc, k0 - 1), P, qp0 + P.sk * (k0 - 1));
+    for (int k = k0; k <= k1; ++k) {
+        const long long q = g.at(ic, jc, k), qp = qp0 + P.sk * k;
+        const double fE = cflux_x(c, q, P, qp);
+        double fW = __shfl_up_sync(0xffffffffu, fE, 1);
+        if (tx == 0) fW = cflux_x(c, q - 1, P, qp - 1);
+        const double fN = cflux_y(c, q, P, qp);
+        sN[ty][tx] = fN;
+        __syncthreads();
+        const double fS = ty > 0 ? sN[ty - 1][tx] : cflux_y(c, q - g.sj, P, qp - P.sj);
+        __syncthreads();
+        const double fF = cflux_z(c, q, P, qp);
+        if (act) {
+            const long long qr = (i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
+            const double r = ((fE - fW) + (fN - fS) + (fF - fB)) - rhs[qr];
+            if (rout) rout[qr] = r;
+            s += r * r;
+            m = fmax(m, fabs(r));
+        }
+        fB = fF;
+    }
+    block_reduce_sum_max(s, m);
+    if (threadIdx.x == 0) {
+        const long long blk = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        part[blk] = s;
+        part[maxoff + blk] = m;
+    }
+}
+
+// Device address of g_norm_scratch on the handle's device (current when this
+// runs).  The first call on each device looks it up with
+// cudaGetSymbolAddress, which may load the module on that device; later
+// calls reuse the cached address.
+int norm_scratch(ples_mg_handle* h, double** out) {
+    static std::mutex mu;
+    static double* addr[kNormMaxDevices] = {};
+    if (h->dev < 0 || h->dev >= kNormMaxDevices)
+        return fail(h, PLES_MG_BAD_ARG, "device %d: the residual scratch serves devices 0..%d", h->dev,
+                    kNormMaxDevices - 1);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[h->dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_norm_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(h, PLES_MG_CUDA_ERROR, "cudaGetSymbolAddress(residual scratch): %s", cudaGetErrorString(e));
+        addr[h->dev] = static_cast<double*>(p);
+    }
+    *out = addr[h->dev];
+    return PLES_MG_OK;
+}
+
+}  // namespace
+
+extern "C" int ples_mg_residual_norms_device(ples_mg_handle* h, const double* d_fi, const double* d_rhs,
+                                             double* d_r, void* stream, double norms[2]) {
+    if (!h || !d_fi || !d_rhs || !norms) return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        const Geom& g = h->L[0].g;
+        const dim3 grd((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kNormKC - 1) / kNormKC);
+        const long long nblk = (long long)grd.x * grd.y * grd.z;
+        if (nblk > kNormMaxBlocks)
+            return fail(h, PLES_MG_BAD_ARG,
+                        "grid %dx%dx%d needs %lld residual blocks; the static scratch holds %d (about 512^3 cells)",
+                        g.nx, g.ny, g.nz, nblk, kNormMaxBlocks);
+        double* part = nullptr;
+        int rc = norm_scratch(h, &part);
+        if (rc) return rc;
+        cudaStream_t st = stream ? (cudaStream_t)stream : h->st;
+        const CompactP P{d_fi, g.nx + 2, (long long)(g.nx + 2) * (g.ny + 2)};
+        k_resid_norm_compact<kNormKC><<<grd, 256, 0, st>>>(g, h->L[0].cd, P, d_rhs, d_r, part, kNormMaxBlocks);
+        k_reduce_final<<<1, 1024, 0, st>>>(part, part + kNormMaxBlocks, nblk, part + 2 * kNormMaxBlocks);
+        h->launches += 2;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(norms, part + 2 * kNormMaxBlocks, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return PLES_MG_OK;
+    });
+}

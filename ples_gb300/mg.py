@@ -60,7 +60,7 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_strerror", "ples_mg_last_error", "ples_mg_levels", "ples_mg_level_dims",
            "ples_mg_get_metric", "ples_mg_apply_residual", "ples_mg_apply_ghost_fill",
            "ples_mg_apply_restrict", "ples_mg_apply_prolong", "ples_mg_counters",
-           "ples_mg_kernel_timing", "ples_mg_kernel_time")
+           "ples_mg_kernel_timing", "ples_mg_kernel_time", "ples_mg_residual_norms_device")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -94,6 +94,7 @@ def load(build=True):
     L.ples_mg_counters.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.ples_mg_kernel_timing.argtypes = [vp, C.c_int, C.c_int]
     L.ples_mg_kernel_time.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    L.ples_mg_residual_norms_device.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_double)]
     _lib = L
     return L
 
@@ -215,6 +216,16 @@ class Multigrid:
                                           C.byref(st))
         self._check(rc, allow=(OK, NOT_CONVERGED))
         return st.as_dict()
+
+    def residual_norms_device(self, d_fi, d_rhs, d_r=0, stream=0):
+        """Fine-level r = L(fi) - rhs from device buffers (integer device
+        pointers, Fortran layout) without any device allocation; returns
+        (sum of r^2, max |r|) and writes r to d_r unless it is 0."""
+        out = (C.c_double * 2)()
+        self._check(self._L.ples_mg_residual_norms_device(
+            self._h, C.c_void_p(int(d_fi)), C.c_void_p(int(d_rhs)), C.c_void_p(int(d_r) or None),
+            C.c_void_p(int(stream) or None), out))
+        return out[0], out[1]
 
     # -- instrumentation ------------------------------------------------------
     def counters(self):
