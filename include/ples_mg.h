@@ -62,7 +62,8 @@ typedef struct {
     int nu_coarse;         /* sweeps on the coarsest level (0 = default)            */
     int inner_cycles;      /* V-cycles per outer FP64 iteration (0 = default)       */
     int smoother;          /* 0 = zebra eta-line SOR (Gauss-Seidel in x and z as the
-                              reference's line SOR), 1 = eta-line Jacobi         */
+                              reference's line SOR); 1 = eta-line Jacobi;
+                              2 = zebra with its rows staged by TMA (FP32) */
     int coarsening;        /* 0 = full, the reference's hierarchy (mul_met);
                               1 = semi-coarsening where x/z spacings differ     */
 } ples_mg_desc;

@@ -154,92 +154,62 @@ __global__ void k_ghost_xz(Geom g, T* __restrict__ p) {
 }
 
 // ---------------------------------------------------------------------------
-// One row of the eta-line system of line (i,k) (solut_sndrcv_slor,
-// multigrid.f03:2126-2198 with sett.f03:114-143).  Rows 0 and ny+1 are the
-// wall ghost relations (homogeneous, an = 0: the smoother runs on
-// corrections; the FP64 outer loop applies the cs terms):
-//   row 0     : A2(0) p0 - A2(0) p1             = B21(0) X0 + B23(0) Z0
-//   row j     : A2(j-1) p(j-1) + b p(j) + A2(j) p(j+1) = rh - N(off-line)
-//   row ny+1  : -A2(ny) p(ny) + A2(ny) p(ny+1)  = -(B21(ny) X + B23(ny) Z)
-// with b = -(A2(j)+A2(j-1)+A1(i)+A1(i-1)+A3(k)+A3(k-1)); every off-line
-// neighbour and every cross term is explicit.  Outputs: f, the diagonal b
-// and a2 = A2 of face j (the coupling of rows j and j+1).  ZERO: p == 0.
-template <typename T, bool ZERO>
-__device__ __forceinline__ void line_row(const Geom& g, const Coef<T>& c, const T* __restrict__ p,
-                                         const T* __restrict__ rh, int i, int j, int k, T& f, T& b, T& a2) {
-    const long long sj = g.sj, sk = g.sk;
-    const long long q = g.at(i, j, k);
-    if (j == 0) {
-        a2 = ld(c.a2, q);
-        b = a2;
-        f = ZERO ? T(0)
-                 : ld(c.b21, q) * (ld(p, q + 1 + sj) + ld(p, q + 1) - ld(p, q - 1 + sj) - ld(p, q - 1)) +
-                       ld(c.b23, q) * (ld(p, q + sj + sk) + ld(p, q + sk) - ld(p, q + sj - sk) - ld(p, q - sk));
-        return;
-    }
-    if (j == g.ny + 1) {
-        const long long qn = q - sj;
-        a2 = T(0);
-        b = ld(c.a2, qn);
-        f = ZERO ? T(0)
-                 : -(ld(c.b21, qn) * (ld(p, q + 1) + ld(p, qn + 1) - ld(p, q - 1) - ld(p, qn - 1)) +
-                     ld(c.b23, qn) * (ld(p, q + sk) + ld(p, qn + sk) - ld(p, q - sk) - ld(p, qn - sk)));
-        return;
-    }
-    const T a1e = ld(c.a1, q), a1w = ld(c.a1, q - 1);
-    const T a3f = ld(c.a3, q), a3b = ld(c.a3, q - sk);
-    a2 = ld(c.a2, q);
-    b = -(a2 + ld(c.a2, q - sj) + a1e + a1w + a3f + a3b);
-    if (ZERO) {
-        f = ld(rh, q);
-        return;
-    }
-    const T pe = ld(p, q + 1), pw = ld(p, q - 1);
-    const T pn = ld(p, q + sj), ps = ld(p, q - sj);
-    const T pf = ld(p, q + sk), pb = ld(p, q - sk);
-    const T pen = ld(p, q + 1 + sj), pes = ld(p, q + 1 - sj), pwn = ld(p, q - 1 + sj), pws = ld(p, q - 1 - sj);
-    const T pef = ld(p, q + 1 + sk), peb = ld(p, q + 1 - sk), pwf = ld(p, q - 1 + sk), pwb = ld(p, q - 1 - sk);
-    const T pnf = ld(p, q + sj + sk), pnb = ld(p, q + sj - sk), psf = ld(p, q - sj + sk), psb = ld(p, q - sj - sk);
-    T nsum = a1e * pe + a1w * pw + a3f * pf + a3b * pb;
-    nsum += ld(c.b12, q) * (pen + pn - pes - ps) - ld(c.b12, q - 1) * (pn + pwn - ps - pws);
-    nsum += ld(c.b13, q) * (pef + pf - peb - pb) - ld(c.b13, q - 1) * (pf + pwf - pb - pwb);
-    nsum += ld(c.b21, q) * (pen + pe - pwn - pw) - ld(c.b21, q - sj) * (pe + pes - pw - pws);
-    nsum += ld(c.b23, q) * (pnf + pf - pnb - pb) - ld(c.b23, q - sj) * (pf + psf - pb - psb);
-    nsum += ld(c.b31, q) * (pef + pe - pwf - pw) - ld(c.b31, q - sk) * (pe + peb - pw - pwb);
-    nsum += ld(c.b32, q) * (pnf + pn - psf - ps) - ld(c.b32, q - sk) * (pn + pnb - ps - psb);
-    f = ld(rh, q) - nsum;
-}
-
+// The two first-order recurrences of a Thomas solve with a precomputed LU
+// factor, for the 32 lines (lanes) held in shared memory [nj][32]:
+//   forward  d(j) = G(j) - AL(j) d(j-1),  d(0) = G(0)
+//   backward x(j) = d(j) - CP(j) x(j+1),  x(nj-1) = d(nj-1)  (CP(nj-1) = 0)
+// Each is an affine map per row, so the rows are cut into one segment per
+// warp: every warp composes its segment's map (offset u, factor v) with the
+// incoming value set to zero, the maps are shared through su/sv ([nw][32]),
+// each warp folds the maps of the segments before it into its incoming value
+// and then runs its own segment again with that value.  The serial depth
+// drops from 2 nj to about 4 nj / nw + 2 nw dependent steps.  The solution
+// replaces G.  Lanes with mine == false do no arithmetic; every thread must
+// call (the function holds __syncthreads).
 template <typename T>
-__device__ __forceinline__ T rcp(T x) { return T(1) / x; }
-
-// Thomas sweep over rows 0..ny+1 held in shared arrays with stride `st`:
-// f (in: right-hand side, out: solution), b (in: diagonal, scratch), a2
-// (A2 of face j).  tridag.f03:2-32 on the system described at line_row.
-template <typename T>
-__device__ __forceinline__ void thomas(int ny, T* f, T* b, const T* a2, int st) {
-    T cp = T(-1);  // c'_0 = -A2(0)/A2(0)
-    T dp = f[0] / b[0];
-    b[0] = cp;
-    f[0] = dp;
-    for (int j = 1; j <= ny; ++j) {
-        const T a = a2[(j - 1) * st], cc = a2[j * st];
-        const T inv = rcp(b[j * st] - a * cp);
-        cp = cc * inv;
-        dp = (f[j * st] - a * dp) * inv;
-        b[j * st] = cp;
-        f[j * st] = dp;
-    }
-    {
-        const T a = -a2[ny * st];  // row ny+1: sub-diagonal -A2(ny), diagonal A2(ny)
-        const T x = (f[(ny + 1) * st] - a * dp) / (b[(ny + 1) * st] - a * cp);
-        f[(ny + 1) * st] = x;
-        T xs = x;
-        for (int j = ny; j >= 0; --j) {
-            xs = f[j * st] - b[j * st] * xs;
-            f[j * st] = xs;
+__device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int nj, bool mine, T* su, T* sv) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int len = (nj + nw - 1) / nw;
+    const int j0 = min(w * len, nj), j1 = min(j0 + len, nj);
+    T u = T(0), v = T(1);
+    if (mine)
+        for (int j = j0; j < j1; ++j) {
+            const T al = AL[j * 32 + lane];
+            u = G[j * 32 + lane] - al * u;
+            v = -al * v;
+        }
+    su[w * 32 + lane] = u;
+    sv[w * 32 + lane] = v;
+    __syncthreads();
+    if (mine) {
+        T d = T(0);
+        for (int s = 0; s < w; ++s) d = su[s * 32 + lane] + sv[s * 32 + lane] * d;
+        for (int j = j0; j < j1; ++j) {
+            d = G[j * 32 + lane] - AL[j * 32 + lane] * d;
+            G[j * 32 + lane] = d;
         }
     }
+    u = T(0);
+    v = T(1);
+    if (mine)
+        for (int j = j1 - 1; j >= j0; --j) {
+            const T c = CP[j * 32 + lane];
+            u = G[j * 32 + lane] - c * u;
+            v = -c * v;
+        }
+    __syncthreads();  // the forward maps are read by now
+    su[w * 32 + lane] = u;
+    sv[w * 32 + lane] = v;
+    __syncthreads();
+    if (mine) {
+        T x = T(0);
+        for (int s = nw - 1; s > w; --s) x = su[s * 32 + lane] + sv[s * 32 + lane] * x;
+        for (int j = j1 - 1; j >= j0; --j) {
+            x = G[j * 32 + lane] - CP[j * 32 + lane] * x;
+            G[j * 32 + lane] = x;
+        }
+    }
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -266,13 +236,105 @@ __global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp) {
 }
 
 // ---------------------------------------------------------------------------
+// Zebra second half: the odd-i lines of a tile add their six in-plane
+// x-neighbour terms, evaluated with the new even-i values (G holds them;
+// outside the tile the old field pin), to the scaled right-hand side
+// G(j) -= T_x(j) / m(j), where CP(j) held 1/m(j); CP(j) becomes c'(j).
+// Rows go in batches of kXB per warp with every load of a batch issued
+// before its arithmetic.  Loads of rows 0 and ny+1 that the wall relations
+// do not use stay inside the box allocation (k >= 1).
+template <typename T, bool ZIN>
+__device__ __forceinline__ void odd_x_terms(const Geom& g, const Coef<T>& c, const T* __restrict__ cpa,
+                                            const T* __restrict__ pin, T* G, T* CP, int i, int k) {
+    constexpr int kXB = 2;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nj = g.ny + 2, ny = g.ny;
+    const long long sj = g.sj, sk = g.sk;
+    const bool west_out = lane == 0 || i - 1 < 1;  // i-1 not a lane of this tile
+    auto PX = [&](int j, int di, int dj) -> T {
+        const int l2 = lane + di;
+        if (l2 >= 0 && l2 < 32 && i + di >= 1 && i + di <= g.nx) return G[(j + dj) * 32 + l2];
+        return ZIN ? T(0) : ld(pin, g.at(i + di, j + dj, k));
+    };
+    for (int jb = w; jb < nj; jb += kXB * nw) {
+        T a1[kXB], a1w[kXB], b12[kXB], b12w[kXB], b21[kXB], b21s[kXB], b31[kXB], b31b[kXB], cpv[kXB];
+        T wm[kXB], w0[kXB], wp[kXB];  // old west neighbours (dj = -1, 0, +1) when outside the tile
+#pragma unroll
+        for (int u = 0; u < kXB; ++u) {
+            const int j = min(jb + u * nw, nj - 1);
+            const long long q = g.at(i, j, k);
+            a1[u] = ld(c.a1, q); a1w[u] = ld(c.a1, q - 1);
+            b12[u] = ld(c.b12, q); b12w[u] = ld(c.b12, q - 1);
+            b21[u] = ld(c.b21, q); b21s[u] = ld(c.b21, q - sj);
+            b31[u] = ld(c.b31, q); b31b[u] = ld(c.b31, q - sk);
+            cpv[u] = ld(cpa, q);
+            const bool wl = !ZIN && west_out;
+            wm[u] = wl && j > 0 ? ld(pin, q - 1 - sj) : T(0);
+            w0[u] = wl ? ld(pin, q - 1) : T(0);
+            wp[u] = wl && j < nj - 1 ? ld(pin, q - 1 + sj) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kXB; ++u) {
+            const int j = jb + u * nw;
+            if (j >= nj) break;
+            const T pw = west_out ? w0[u] : PX(j, -1, 0);
+            const T pwn = west_out ? wp[u] : (j < nj - 1 ? PX(j, -1, 1) : T(0));
+            const T pws = west_out ? wm[u] : (j > 0 ? PX(j, -1, -1) : T(0));
+            T tx;
+            if (j == 0) {
+                tx = -b21[u] * (PX(j, 1, 1) + PX(j, 1, 0) - pwn - pw);
+            } else if (j == ny + 1) {
+                tx = b21s[u] * (PX(j, 1, 0) + PX(j, 1, -1) - pw - pws);
+            } else {
+                const T pe = PX(j, 1, 0);
+                const T pen = PX(j, 1, 1), pes = PX(j, 1, -1);
+                tx = a1[u] * pe + a1w[u] * pw + b12[u] * (pen - pes) - b12w[u] * (pwn - pws) +
+                     b21[u] * (pen + pe - pwn - pw) - b21s[u] * (pe + pes - pw - pws) + (b31[u] - b31b[u]) * (pe - pw);
+            }
+            const T im = CP[j * 32 + lane];
+            G[j * 32 + lane] -= tx * im;
+            CP[j * 32 + lane] = j == ny + 1 ? T(0) : cpv[u];
+        }
+    }
+}
+
+// Phase 3: relax the rows j = w, w+nw, ... of this lane's line, keep the
+// new value in G (zebra: the odd-i lines read it) and store it with its
+// periodic images.  The old values of a batch of kRB rows are loaded first.
+template <typename T, bool ZEBRA, bool ZIN>
+__device__ __forceinline__ void relax_store(const Geom& g, const T* __restrict__ pin, T* pout, T* G, T omega, int i,
+                                            int k) {
+    constexpr int kRB = 4;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nj = g.ny + 2;
+    for (int jb = w; jb < nj; jb += kRB * nw) {
+        T old[kRB];
+#pragma unroll
+        for (int u = 0; u < kRB; ++u) {
+            const int j = jb + u * nw;
+            old[u] = (!ZIN && j < nj) ? ld(pin, g.at(i, j, k)) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kRB; ++u) {
+            const int j = jb + u * nw;
+            if (j >= nj) break;
+            const T x = G[j * 32 + lane];
+            const T v = ZIN ? omega * x : old[u] + omega * (x - old[u]);
+            if (ZEBRA) G[j * 32 + lane] = v;
+            store_periodic(g, pout, i, j, k, v);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // eta-line relaxation (the device form of solut_sndrcv_slor,
 // multigrid.f03:1939-2290, with tridag.f03).  A CTA owns 32 consecutive
 // lines in i (one per lane) of one plane k, all rows j = 0..ny+1:
 //   phase 1: every warp builds rows j = w, w+W, ... of its lines' systems
 //            (coalesced row loads; off-line neighbours and cross terms
 //            explicit) and stores g = f/m, alpha = a/m, c' (m = b - a c'(j-1))
-//   phase 2: warp 0 runs the two FMA recurrences per line in shared memory
+//   phase 2: all warps run the two FMA recurrences per line in shared
+//            memory, one row segment each (seg_thomas)
 //   phase 3: every warp writes its rows, relaxed, with the periodic images.
 // JACOBI: all lines of all planes from the old field pin -> pout.
 // ZEBRA : the lines with one parity of k (launch argument kpar); inside the
@@ -285,9 +347,9 @@ __global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp) {
 //         Own-plane old values come from pin, k+-1 planes from pk (= pin for
 //         the first parity, = pout for the second); output to pout.
 // ZIN: pin is identically zero (first sweep of a correction); zk: pk is too.
-// Shared memory: 3 arrays [ny+2][32].
+// Shared memory: 3 arrays [ny+2][32] and the segment maps [2][8][32].
 template <typename T, bool ZEBRA, bool ZIN>
-__global__ void __launch_bounds__(256) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
                                                     int kpar, int zk) {
@@ -308,12 +370,6 @@ __global__ void __launch_bounds__(256) k_line_relax(Geom g, Coef<T> c, const T* 
         const long long q = g.at(i + di, j + dj, k + dk);
         if (dk != 0) return zk ? T(0) : ld(pk, q);
         return ZIN ? T(0) : ld(pin, q);
-    };
-    // in-plane x-neighbour after the even-i update (odd lanes, second half)
-    auto PX = [&](int j, int di, int dj) -> T {
-        const int l2 = lane + di;
-        if (l2 >= 0 && l2 < 32 && i + di >= 1 && i + di <= g.nx) return G[(j + dj) * 32 + l2];
-        return ZIN ? T(0) : ld(pin, g.at(i + di, j + dj, k));
     };
     const bool noneigh = ZIN && (!ZEBRA || zk);  // every old neighbour is zero
     if (act) {
@@ -386,58 +442,15 @@ __global__ void __launch_bounds__(256) k_line_relax(Geom g, Coef<T> c, const T* 
             CP[j * 32 + lane] = odd ? im : (j == ny + 1 ? T(0) : ld(cpa, q));
         }
     }
+    T* SU = CP + nj * 32;  // segment maps of the parallel Thomas solve
+    T* SV = SU + nw * 32;
     const int nhalf = ZEBRA ? 2 : 1;
     for (int half = 0; half < nhalf; ++half) {
         const bool mine = act && (!ZEBRA || ((i & 1) == half));
-        if (ZEBRA && half == 1 && mine) {  // in-plane x-neighbour terms with the new even-i values
-            for (int j = w; j < nj; j += nw) {
-                const long long q = g.at(i, j, k);
-                T tx;
-                if (j == 0) {
-                    tx = -ld(c.b21, q) * (PX(j, 1, 1) + PX(j, 1, 0) - PX(j, -1, 1) - PX(j, -1, 0));
-                } else if (j == ny + 1) {
-                    tx = ld(c.b21, q - sj) * (PX(j, 1, 0) + PX(j, 1, -1) - PX(j, -1, 0) - PX(j, -1, -1));
-                } else {
-                    const T pe = PX(j, 1, 0), pw = PX(j, -1, 0);
-                    const T pen = PX(j, 1, 1), pes = PX(j, 1, -1), pwn = PX(j, -1, 1), pws = PX(j, -1, -1);
-                    const T b12 = ld(c.b12, q), b12w = ld(c.b12, q - 1);
-                    tx = ld(c.a1, q) * pe + ld(c.a1, q - 1) * pw + b12 * (pen - pes) - b12w * (pwn - pws) +
-                         ld(c.b21, q) * (pen + pe - pwn - pw) - ld(c.b21, q - sj) * (pe + pes - pw - pws) +
-                         (ld(c.b31, q) - ld(c.b31, q - sk)) * (pe - pw);
-                }
-                const T im = CP[j * 32 + lane];
-                G[j * 32 + lane] -= tx * im;
-                CP[j * 32 + lane] = j == ny + 1 ? T(0) : ld(cpa, q);
-            }
-        }
+        if (ZEBRA && half == 1 && mine) odd_x_terms<T, ZIN>(g, c, cpa, pin, G, CP, i, k);
         __syncthreads();
-        if (w == 0 && mine) {
-            T d = G[lane];
-            for (int j = 1; j < nj; ++j) {
-                d = G[j * 32 + lane] - AL[j * 32 + lane] * d;
-                G[j * 32 + lane] = d;
-            }
-            T x = d;
-            for (int j = nj - 2; j >= 0; --j) {
-                x = G[j * 32 + lane] - CP[j * 32 + lane] * x;
-                G[j * 32 + lane] = x;
-            }
-        }
-        __syncthreads();
-        if (mine) {
-            for (int j = w; j < nj; j += nw) {
-                const T x = G[j * 32 + lane];
-                T v;
-                if (ZIN) {
-                    v = omega * x;
-                } else {
-                    const T old = ld(pin, g.at(i, j, k));
-                    v = old + omega * (x - old);
-                }
-                if (ZEBRA) G[j * 32 + lane] = v;
-                store_periodic(g, pout, i, j, k, v);
-            }
-        }
+        seg_thomas(G, AL, CP, nj, mine, SU, SV);
+        if (mine) relax_store<T, ZEBRA, ZIN>(g, pin, pout, G, omega, i, k);
         if (ZEBRA) __syncthreads();
     }
 }

@@ -23,6 +23,7 @@
 #include <string>
 #include <vector>
 
+#include "line_tma.cuh"
 #include "mg_device.cuh"
 #include "metric.h"
 #include "ples_mg.h"
@@ -333,6 +334,11 @@ struct LevelData {
     Coef<float> cf{};             // FP32 scaled coefficients (mixed)
     Coef<double> cd{};            // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
     bool has_cf = false, has_cd = false;
+    // TMA-staged zebra smoother (FP32): tensor maps of this level's fields;
+    // pA/pB are the buffers behind maps.pA/pB (p and p2 swap every sweep)
+    bool tma = false;
+    void *pA = nullptr, *pB = nullptr;
+    LineMaps maps{};
 };
 
 struct ples_mg_handle {
@@ -346,7 +352,8 @@ struct ples_mg_handle {
     double* wbuf = nullptr;                              // 2*nx*nz wall rows
     double *part_a = nullptr, *part_b = nullptr;         // block partials
     long long npart = 0;
-    double* red = nullptr;                               // 2 doubles on the device
+    double* red = nullptr;                               // 2 doubles on the device (+ dflag)
+    int* dflag = nullptr;                                // bounded-wait error flag, inside red
     double* h_red = nullptr;                             // pinned host copy
     double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
     double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes
@@ -489,7 +496,7 @@ void ghost_xz(ples_mg_handle* h, const Geom& g, T* p) {
 }
 
 template <typename T>
-size_t line_smem(const Geom& g) { return 3 * (size_t)(g.ny + 2) * 32 * sizeof(T); }
+size_t line_smem(const Geom& g) { return (3 * (size_t)(g.ny + 2) + 2 * 8) * 32 * sizeof(T); }
 
 // the dynamic shared-memory limit is a per-function attribute shared by all
 // handles of the process: only ever raise it
@@ -506,6 +513,75 @@ int set_smem_attrs(ples_mg_handle* h, size_t smem) {
     return 0;
 }
 
+int set_tma_smem_attr(ples_mg_handle* h, size_t smem) {
+    static size_t current = 0;
+    if (smem <= current) return 0;
+    current = smem;
+    CK(cudaFuncSetAttribute(k_line_relax_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return 0;
+}
+
+// cuTensorMapEncodeTiled, fetched once through the runtime's driver entry point
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int tensor_encoder(ples_mg_handle* h, EncodeTiledFn* fn) {
+    static std::mutex mu;
+    static EncodeTiledFn cached = nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cached) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p)
+            return fail(h, PLES_MG_CUDA_ERROR, "cuTensorMapEncodeTiled is not available from the driver");
+        cached = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    *fn = cached;
+    return PLES_MG_OK;
+}
+
+// 3-D map of one FP32 box field of geometry g (x = element of the padded
+// row, y = j, z = k), box bx x by x bz, zero fill outside
+int encode_box(ples_mg_handle* h, EncodeTiledFn enc, CUtensorMap* m, const void* base, const Geom& g, unsigned bx,
+               unsigned by, unsigned bz) {
+    const cuuint64_t dims[3] = {(cuuint64_t)g.sj, (cuuint64_t)g.ny + 2, (cuuint64_t)g.nz + 2};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.sj * 4, (cuuint64_t)g.sk * 4};
+    const cuuint32_t box[3] = {bx, by, bz};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(h, PLES_MG_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return PLES_MG_OK;
+}
+
+// the boxes k_line_relax_tma reads, for one FP32 level
+int build_line_maps(ples_mg_handle* h, LevelData& L) {
+    EncodeTiledFn enc = nullptr;
+    int rc = tensor_encoder(h, &enc);
+    if (rc) return rc;
+    const Geom& g = L.g;
+    const unsigned R = kRC;
+    LineMaps& M = L.maps;
+    const Coef<float>& c = L.cf;
+    if ((rc = encode_box(h, enc, &M.pA, L.p, g, 40, R + 2, 1)) || (rc = encode_box(h, enc, &M.pB, L.p2, g, 40, R + 2, 1)) ||
+        (rc = encode_box(h, enc, &M.a1, c.a1, g, 36, R, 1)) || (rc = encode_box(h, enc, &M.b12, c.b12, g, 36, R, 1)) ||
+        (rc = encode_box(h, enc, &M.b13, c.b13, g, 36, R, 1)) ||
+        (rc = encode_box(h, enc, &M.a2, c.a2, g, 32, R + 1, 1)) ||
+        (rc = encode_box(h, enc, &M.b21, c.b21, g, 32, R + 1, 1)) ||
+        (rc = encode_box(h, enc, &M.b23, c.b23, g, 32, R + 1, 1)) || (rc = encode_box(h, enc, &M.a3, c.a3, g, 32, R, 2)) ||
+        (rc = encode_box(h, enc, &M.b31, c.b31, g, 32, R, 2)) || (rc = encode_box(h, enc, &M.b32, c.b32, g, 32, R, 2)) ||
+        (rc = encode_box(h, enc, &M.rh, L.rh, g, 32, R, 1)) || (rc = encode_box(h, enc, &M.cp, L.cp, g, 32, R + 1, 1)))
+        return rc;
+    L.pA = L.p;
+    L.pB = L.p2;
+    L.tma = true;
+    return PLES_MG_OK;
+}
+
 // nu sweeps; `zero` = the field is identically zero before the first sweep
 template <typename T>
 void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
@@ -519,7 +595,29 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
         const T* pin = (const T*)L.p;
         T* pout = (T*)L.p2;
         timed_begin(h, KIND_LINE, level);
-        if (h->smoother == 0) {  // zebra: two launches, k parities
+        bool staged = false;
+        if constexpr (std::is_same<T, float>::value) {
+            if (L.tma) {  // zebra with TMA-staged rows
+                dim3 grd((L.g.nz + 1) / 2, (L.g.nx + 31) / 32);
+                const size_t sm = line_tma_smem(L.g.ny);
+                const int a_in = pin == L.pA, a_out = pout == L.pA;
+                if (zin) {
+                    k_line_relax_tma<true><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 0, 1, a_in,
+                                                                     a_in, h->dflag);
+                    k_line_relax_tma<true><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 1, 0, a_in,
+                                                                     a_out, h->dflag);
+                } else {
+                    k_line_relax_tma<false><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 0, 0, a_in,
+                                                                      a_in, h->dflag);
+                    k_line_relax_tma<false><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 1, 0, a_in,
+                                                                      a_out, h->dflag);
+                }
+                h->launches += 2;
+                staged = true;
+            }
+        }
+        if (staged) {
+        } else if (h->smoother != 1) {  // zebra: two launches, k parities
             dim3 grd((L.g.nz + 1) / 2, (L.g.nx + 31) / 32);
             if (zin) {
                 k_line_relax<T, true, true><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
@@ -593,11 +691,18 @@ int reduce_to_host(ples_mg_handle* h, const double* a, const double* bmax, long 
     k_reduce_final<<<1, 1024, 0, h->st>>>(a, bmax, n, h->red);
     ++h->launches;
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h->h_red, h->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    // the two results and the bounded-wait flag behind them
+    CK(cudaMemcpyAsync(h->h_red, h->red, 5 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     timed_collect(h);
     out[0] = h->h_red[0];
     out[1] = h->h_red[1];
+    int flag = 0;
+    std::memcpy(&flag, h->h_red + 4, sizeof flag);
+    if (flag) {
+        CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
+        return fail(h, PLES_MG_DEVICE_TIMEOUT, "a staged transfer of the line smoother did not complete");
+    }
     return PLES_MG_OK;
 }
 
@@ -738,7 +843,7 @@ int validate(const ples_mg_desc* d, ples_mg_handle* h) {
     if (!(d->dt > 0.0) || !std::isfinite(d->dt)) return fail(h, PLES_MG_BAD_ARG, "dt must be positive");
     if (d->nlevmax < 0 || d->nu_pre < 0 || d->nu_post < 0 || d->nu_coarse < 0 || d->inner_cycles < 0)
         return fail(h, PLES_MG_BAD_ARG, "negative level or sweep count");
-    if (d->smoother != 0 && d->smoother != 1) return fail(h, PLES_MG_BAD_ARG, "unknown smoother %d", d->smoother);
+    if (d->smoother < 0 || d->smoother > 2) return fail(h, PLES_MG_BAD_ARG, "unknown smoother %d", d->smoother);
     if (d->coarsening != 0 && d->coarsening != 1)
         return fail(h, PLES_MG_BAD_ARG, "unknown coarsening %d", d->coarsening);
     if (d->jx % 2 || d->jz % 2) return fail(h, PLES_MG_BAD_ARG, "jx and jz must be even");
@@ -896,7 +1001,7 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     CK(cudaSetDevice(h->dev));
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     h->smoother = d->smoother;
-    h->omega = d->omega > 0.0 ? d->omega : (d->smoother == 0 ? 1.3 : 0.8);
+    h->omega = d->omega > 0.0 ? d->omega : (d->smoother != 1 ? 1.3 : 0.8);
     h->nu_pre = d->nu_pre ? d->nu_pre : 2;
     h->nu_post = d->nu_post ? d->nu_post : 2;
     h->nu_coarse = d->nu_coarse ? d->nu_coarse : 40;
@@ -996,6 +1101,9 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         CK(cudaGetLastError());
         size_t sm = mixed ? line_smem<float>(L.g) : line_smem<double>(L.g);
         smem_max = std::max(smem_max, sm);
+        if (mixed && h->smoother == 2 && line_tma_smem(L.g.ny) <= 227 * 1024) {
+            if ((rc = build_line_maps(h, L)) || (rc = set_tma_smem_attr(h, line_tma_smem(L.g.ny)))) return rc;
+        }
     }
     {
         const LevelData& C = h->L[nl - 1];
@@ -1017,6 +1125,8 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     if ((rc = dalloc(h, (void**)&h->part_a, 8 * (size_t)h->npart)) ||
         (rc = dalloc(h, (void**)&h->part_b, 8 * (size_t)h->npart)) || (rc = dalloc(h, (void**)&h->red, 64)))
         return rc;
+    h->dflag = reinterpret_cast<int*>(h->red + 4);
+    CK(cudaMemsetAsync(h->red, 0, 64, h->st));
     CK(cudaMallocHost((void**)&h->h_red, 64));
     const size_t nfi = (size_t)(jx + 2) * (jy + 2) * (jz + 2), nrh = (size_t)jx * jy * jz;
     if ((rc = dalloc(h, (void**)&h->fi_c, 8 * nfi)) || (rc = dalloc(h, (void**)&h->rhs_c, 8 * nrh))) return rc;

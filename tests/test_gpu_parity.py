@@ -215,6 +215,24 @@ def test_jacobi_smoother_same_solution(case0):
     assert l2 <= SOL_TOL and mx <= SOL_TOL
 
 
+def test_staged_and_plain_zebra_agree(case0):
+    """The zebra smoother with plain loads (default) and the same smoother
+    with its rows staged by TMA (FP32) compute the same sweeps: same cycle
+    counts and the same converged solution."""
+    out = {}
+    for sm in (0, 2):
+        with mg.Multigrid(case0["x"], case0["y"], case0["z"], smoother=sm) as m:
+            fi, st = m.solve(case0["rhs"], rel_tol=REL_TOL)
+        assert st["status"] == mg.OK
+        out[sm] = (fi, st)
+    assert out[0][1]["vcycles"] == out[2][1]["vcycles"]
+    assert abs(out[0][1]["rel_residual"] - out[2][1]["rel_residual"]) <= 1e-3 * out[2][1]["rel_residual"]
+    l2, mx = _rel(_zm(out[0][0]), _zm(out[2][0]))
+    assert l2 <= 1e-10 and mx <= 1e-10
+    l2, mx = _rel(_zm(out[0][0]), case0["ref"])
+    assert l2 <= SOL_TOL and mx <= SOL_TOL
+
+
 def test_odd_level_counts_and_small_grids():
     for dims in ((48, 32, 48), (16, 8, 16), (32, 64, 32)):
         x, y, z = S.wavy_channel_grid(*dims, 0.05, 1.5)
