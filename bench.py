@@ -207,6 +207,11 @@ def main():
     ap.add_argument("--nu", type=int, default=0)
     ap.add_argument("--inner", type=int, default=0)
     ap.add_argument("--omega", type=float, default=0.0)
+    ap.add_argument("--batch-steps", type=int, default=3,
+                    help="timed repetitions of the 64-grid batched solve (0: skip that leg)")
+    ap.add_argument("--serve-requests", type=int, default=400,
+                    help="requests of the served-ensemble leg (0: skip that leg)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -285,8 +290,13 @@ def main():
     e2e_value = None
     if args.e2e_steps > 0:
         e2e_value = e2e_leg(args, m, rhs, w, nfi) * ws
+    extra = {}
+    if args.batch_steps > 0:
+        extra["batch"] = batch_leg(args, local)
+    if args.serve_requests > 0:
+        extra["serve"] = serve_leg(args, local)
     _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, st64, err_vs_fp64,
-            e2e_value, nfi, launches, kms, kn, clk)
+            e2e_value, nfi, launches, kms, kn, clk, extra)
 
 
 def fp64_leg(args, x, y, z, w, nfi, d_fi, d_rhs, local, sh):
@@ -348,8 +358,142 @@ def e2e_leg(args, m, rhs, w, nfi):
     return 1.0 / te  # per replica
 
 
+def batch_leg(args, local):
+    """64 independent grids of uneven size (seeds 2..65) solved together by
+    one batch (a captured graph of persistent step kernels per outer
+    iteration), against the same 64 grids solved one after another by the
+    plain FP64 solver and by the single-grid mixed solver.  Device-resident
+    inputs; wall-clock time of whole calls (each returns after its solves)."""
+    import numpy as np
+    import torch
+    from ples_gb300 import mg
+    from ples_gb300 import synthetic as S
+    insts = S.batch_instances()
+    grids = [w.grid() for w in insts]
+    rhs = [w.rhs() for w in insts]
+    nfis = [(w.jx + 2) * (w.jy + 2) * (w.jz + 2) for w in insts]
+    d_rhs = [torch.from_numpy(np.ascontiguousarray(r.ravel(order="F"))).cuda() for r in rhs]
+    d_fi = [torch.zeros(n, dtype=torch.float64, device="cuda") for n in nfis]
+    members = [mg.Multigrid(*g, device=local) for g in grids]
+    b = mg.Batch(members)
+
+    def run():
+        for f in d_fi:
+            f.zero_()
+        torch.cuda.synchronize()
+        return b.solve_device([f.data_ptr() for f in d_fi], [r.data_ptr() for r in d_rhs], rel_tol=1e-10)
+
+    run()
+    t0 = time.perf_counter()
+    for _ in range(args.batch_steps):
+        sts = run()
+    tb = (time.perf_counter() - t0) / args.batch_steps
+    info = b.info()
+    ok = all(s["status"] == mg.OK for s in sts)
+    relmax = max(s["rel_residual"] for s in sts)
+    # end to end: host arrays in and out
+    t0 = time.perf_counter()
+    b.solve(rhs, rel_tol=1e-10)
+    te = time.perf_counter() - t0
+    b.close()
+    sh = torch.cuda.current_stream().cuda_stream
+
+    def sequential(ms, fs, rs):
+        tot = 0.0
+        for mm, f, r in zip(ms, fs, rs, strict=True):
+            f.zero_()
+            mm.solve_device(f.data_ptr(), r.data_ptr(), rel_tol=1e-10, max_cycles=400, stream=sh)
+            torch.cuda.synchronize()
+            f.zero_()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            mm.solve_device(f.data_ptr(), r.data_ptr(), rel_tol=1e-10, max_cycles=400, stream=sh)
+            torch.cuda.synchronize()
+            tot += time.perf_counter() - t1
+        return tot
+
+    t_mixed_seq = sequential(members, d_fi, d_rhs)
+    for mm in members:
+        mm.close()
+    t_fp64 = 0.0
+    for g, f, r in zip(grids, d_fi, d_rhs):  # one FP64 hierarchy at a time
+        m64 = mg.Multigrid(*g, precision="fp64", device=local)
+        t_fp64 += sequential([m64], [f], [r])
+        m64.close()
+    n = len(insts)
+    return {"instances": n, "cells_total": int(sum(w.cells for w in insts)),
+            "sizes": sorted({f"{w.jx}x{w.jy}x{w.jz}" for w in insts}),
+            "value": n / tb, "unit": "solves/s", "ms_per_batch": tb * 1e3,
+            "e2e": {"value": n / te, "unit": "solves/s", "note": "host arrays, copies inside"},
+            "all_converged": ok, "max_rel_residual": relmax,
+            "steps_per_outer_iteration": info["steps"],
+            "sequential_fp64": {"value": n / t_fp64, "unit": "solves/s", "ms_total": t_fp64 * 1e3},
+            "sequential_mixed": {"value": n / t_mixed_seq, "unit": "solves/s", "ms_total": t_mixed_seq * 1e3},
+            "batch_over_sequential_fp64": t_fp64 / tb}
+
+
+def serve_leg(args, local):
+    """16 ensemble members on fixed grids, requests arriving as a Poisson
+    process, each member's RHS the previous one plus 5% noise, warm starts,
+    continuous batching in the server.  Latency = submission to completion,
+    measured by the server.  Run at the configured aggregate rate and again
+    at 70% of the throughput measured there (latency without a growing
+    queue)."""
+    import numpy as np
+    from ples_gb300 import mg
+    from ples_gb300 import synthetic as S
+    ms = S.serve_members(16)
+    handles = [mg.Multigrid(*w.grid(), device=local) for w in ms]
+    srv = mg.Server(handles, hbm_budget_bytes=150e9)
+    state = [w.rhs() for w in ms]
+    rngs = [np.random.default_rng(2000 + i) for i in range(len(ms))]
+    # warm-up: one cold solve per member
+    for t in [srv.submit(i, state[i]) for i in range(len(ms))]:
+        srv.wait(t)
+
+    def run(rate, n, seed):
+        at, who = S.poisson_arrivals(rate, n, seed=seed, members=len(ms))
+        reqs = []
+        for t, i in zip(at, who):
+            state[i] = S.next_rhs(state[i], rngs[i])
+            reqs.append((float(t), int(i), state[i]))
+        t0 = time.perf_counter()
+        tickets = []
+        for t, i, r in reqs:
+            d = t0 + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets.append(srv.submit(i, r))
+        lat, rel, ok, outer = [], 0.0, True, []
+        for tk in tickets:
+            _, st = srv.wait(tk)
+            lat.append(st["seconds"] * 1e3)
+            rel = max(rel, st["rel_residual"])
+            outer.append(st["outer_iterations"])
+            ok = ok and st["status"] == mg.OK
+        span = time.perf_counter() - t0
+        lat = np.array(lat)
+        return {"offered_rate": rate, "requests": n, "solves_per_s": n / span,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "p999_ms": float(np.percentile(lat, 99.9)), "all_converged": ok, "max_rel_residual": rel,
+                "outer_iterations_mean": float(np.mean(outer))}
+
+    full = run(args.serve_rate, args.serve_requests, 7)
+    rate2 = 0.7 * full["solves_per_s"]
+    light = run(rate2, max(32, int(rate2 * 2.0)), 8)
+    srv.close()
+    for h in handles:
+        h.close()
+    out = {"members": len(ms), "sizes": sorted({f"{w.jx}x{w.jy}x{w.jz}" for w in ms}),
+           "cells_total": int(sum(w.cells for w in ms)), "hbm_budget_bytes": 150e9}
+    out.update(full)
+    out["at_70pct_throughput"] = light
+    out["note"] = "latency includes queueing whenever the offered rate exceeds the throughput"
+    return out
+
+
 def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, st64, err_vs_fp64,
-            e2e_value, nfi, launches, kms, kn, clk):
+            e2e_value, nfi, launches, kms, kn, clk, extra=None):
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -395,6 +539,7 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
         "clocks": clk,
         "cpu_baseline": cpu,
     }
+    out.update(extra or {})
     print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -150,6 +150,55 @@ int ples_mg_counters(ples_mg_handle *h, long long *launches, long long *device_b
 int ples_mg_kernel_timing(ples_mg_handle *h, int kind, int level);
 int ples_mg_kernel_time(ples_mg_handle *h, double *total_ms, long long *launches);
 
+/* ---- many grids at once ------------------------------------------------
+ * No counterpart in the reference, which solves one grid per run.  A batch
+ * groups existing handles (mixed precision, zebra smoother, full
+ * coarsening, nu_pre == nu_post, all on one device); each keeps its
+ * resident hierarchy.  One outer iteration of all members is a captured
+ * CUDA graph of persistent step kernels that walk (member, level, tile)
+ * queues; convergence is decided per member on the device, so members of
+ * different sizes finish independently.  The stop rule is the relative one
+ * of ples_mg_solve (rel_tol), with max_cycles outer iterations. */
+typedef struct ples_mg_batch ples_mg_batch;
+int ples_mg_batch_create(ples_mg_handle *const *members, int n, ples_mg_batch **out);
+/* fi[i] (host, (0:jx+1,0:jy+1,0:jz+1)) in/out, or fi == NULL / fi[i] ==
+ * NULL to start from the member's resident solution and keep the result
+ * on the device; rhs[i] (host, (1:jx,1:jy,1:jz)); stats[n] or NULL.
+ * Returns OK, NOT_CONVERGED or DIVERGED (the worst member) or an error. */
+int ples_mg_batch_solve(ples_mg_batch *b, double *const *fi, const double *const *rhs,
+                        double rel_tol, int max_cycles, ples_mg_stats *stats);
+/* the same with device buffers in the same layouts */
+int ples_mg_batch_solve_device(ples_mg_batch *b, double *const *d_fi, const double *const *d_rhs,
+                               double rel_tol, int max_cycles, ples_mg_stats *stats);
+/* steps (launches) per outer iteration and graph replays so far */
+int ples_mg_batch_info(const ples_mg_batch *b, int *steps, long long *replays);
+const char *ples_mg_batch_last_error(const ples_mg_batch *b);
+void ples_mg_batch_destroy(ples_mg_batch *b);
+
+/* ---- request server with continuous batching ---------------------------
+ * No counterpart in the reference.  A server owns a batch over the member
+ * handles (their resident hierarchies must fit hbm_budget_bytes, else
+ * PLES_MG_OOM; 0 = no budget) and a worker thread.  Requests arrive from
+ * any host thread; a request is admitted as soon as its member has no
+ * request in flight and joins the next outer iteration of the members
+ * already running, so the work of all admitted requests overlaps on the
+ * device.  Each solve starts from its member's previous solution (warm
+ * start; zero for the first).  Thread-safe. */
+typedef struct ples_srv ples_srv;
+int ples_srv_create(ples_mg_handle *const *members, int n, double hbm_budget_bytes, ples_srv **out);
+/* rhs (host, (1:jx,1:jy,1:jz)) is copied before the call returns; fi_out
+ * (host, (0:jx+1,0:jy+1,0:jz+1)) receives the solution and must stay valid
+ * until ples_srv_wait returns for the ticket. */
+int ples_srv_submit(ples_srv *s, int member, const double *rhs, double *fi_out, double rel_tol,
+                    int max_cycles, long long *ticket);
+/* blocks until the request completes; returns its status, stats->seconds =
+ * latency from submission to completion */
+int ples_srv_wait(ples_srv *s, long long ticket, ples_mg_stats *stats);
+/* latency percentiles (ms) and throughput of the completed requests */
+int ples_srv_report(ples_srv *s, double *p50_ms, double *p99_ms, double *p999_ms,
+                    long long *completed, double *solves_per_s);
+void ples_srv_destroy(ples_srv *s);
+
 /* ---- fine-level residual norms without device allocation -------------
  * No counterpart in the reference: it has no device and no allocator to
  * avoid.  For callers that must not allocate device memory during the call

@@ -1,10 +1,11 @@
 """Build the CUDA library libples_mg.so in-tree for GB300 (sm_103a).
 
-Two translation units compiled in parallel with nvcc and linked into one
+Three translation units compiled in parallel with nvcc and linked into one
 shared object under ples_gb300/_build/:
   csrc/metric.cu   -- device face metric, compiled with -fmad=false so its
                       FP64 arithmetic is rounded as written
   csrc/ples_mg.cu  -- stencil kernels, V-cycle driver and the C ABI
+  csrc/batch.cu    -- batched solves of many grids and the request server
 The library depends on the CUDA runtime only (statically linked); PyTorch is
 not needed to build or load it.
 """
@@ -51,7 +52,7 @@ def build(force=False, verbose=False, extra=()):
     nvcc = nvcc_path()
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", SRC,
               "-I", os.path.join(ROOT, "include")] + ARCH + list(extra)
-    units = [("metric.cu", ["-fmad=false"]), ("ples_mg.cu", [])]
+    units = [("metric.cu", ["-fmad=false"]), ("ples_mg.cu", []), ("batch.cu", [])]
     procs = []
     for name, flags in units:
         obj = os.path.join(OUT, name.replace(".cu", ".o"))
@@ -68,7 +69,7 @@ def build(force=False, verbose=False, extra=()):
             print(out.decode(errors="replace"), file=sys.stderr)
         objs.append(obj)
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs
+    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout.decode(errors='replace')}")

@@ -1,0 +1,91 @@
+// handle.h -- the state behind a ples_mg_handle (one grid's coefficient
+// hierarchy and work buffers on one device), shared by the single-grid
+// solver (ples_mg.cu) and the batched engine (batch.cu).  Internal: not part
+// of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "line_tma.cuh"
+#include "mg_device.cuh"
+#include "ples_mg.h"
+
+constexpr int kMaxLev = 12;
+
+struct LevelData {
+    ples::Geom g;
+    int rx = 1, ry = 1, rz = 1;  // coarsening ratio from the finer level
+    int sx = 1, sy = 1, sz = 1;  // cumulative node strides relative to level 1
+    double inv_div = 1.0;        // raw metric = t * inv_div
+    double post = 1.0;           // stored coefficient = raw * post (x 1/4 on cross terms)
+    void* p = nullptr;           // inner-precision fields (T boxes)
+    void* p2 = nullptr;
+    void* rh = nullptr;
+    void* cp = nullptr;          // LU factor c' of the eta-line operator (T box)
+    ples::Coef<float> cf{};             // FP32 scaled coefficients (mixed)
+    ples::Coef<double> cd{};            // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
+    bool has_cf = false, has_cd = false;
+    // TMA-staged zebra smoother (FP32): tensor maps of this level's fields;
+    // pA/pB are the buffers behind maps.pA/pB (p and p2 swap every sweep)
+    bool tma = false;
+    void *pA = nullptr, *pB = nullptr;
+    ples::LineMaps maps{};
+};
+
+struct ples_mg_handle {
+    ples_mg_desc d{};
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    int nlev = 0;
+    LevelData L[kMaxLev];
+    double *xn = nullptr, *yn = nullptr, *zn = nullptr;  // fine nodes (0:jx,0:jy,0:jz)
+    double *x = nullptr, *b = nullptr;                   // FP64 solution / rhs boxes (level 1)
+    double* wbuf = nullptr;                              // 2*nx*nz wall rows
+    double *part_a = nullptr, *part_b = nullptr;         // block partials
+    long long npart = 0;
+    double* red = nullptr;                               // 2 doubles on the device (+ dflag)
+    int* dflag = nullptr;                                // bounded-wait error flag, inside red
+    double* h_red = nullptr;                             // pinned host copy
+    double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
+    double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes
+    double* cs_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // their device buffers
+    void* coarse_S = nullptr;                            // dense inverse of the coarsest system (T)
+    int coarse_n = 0;
+    int wall_passes = 3;
+    double wall_q = 0.0;
+    int nu_pre = 2, nu_post = 2, nu_coarse = 40, inner_cycles = 3, smoother = 0;
+    double omega = 0.8;
+    std::vector<void*> allocs;
+    std::string err;
+    long long bytes = 0;
+    // instrumentation: kernels launched, and optional CUDA-event timing of
+    // one kernel kind at one level (pairs are read back after each solve)
+    long long launches = 0;
+    int timed_kind = -1, timed_level = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    double timed_ms = 0.0;
+    long long timed_launches = 0;
+};
+
+inline int fail(ples_mg_handle* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                               \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? PLES_MG_OOM : PLES_MG_CUDA_ERROR, \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                       \
+    } while (0)

@@ -61,6 +61,18 @@ struct Coef {
     T *a3, *b31, *b32;  // zeta faces
 };
 
+// Block coordinates of one unit of work.  Every kernel body takes them
+// explicitly: a plain launch passes blockIdx/gridDim (hw_blk), a batched
+// launch over many grids hands out virtual blocks of each grid's own launch
+// shape (batch.cu), so both run the same code.
+struct Blk {
+    int x, y, z;
+    int gx, gy, gz;
+};
+__device__ __forceinline__ Blk hw_blk() {
+    return Blk{(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y, (int)gridDim.z};
+}
+
 template <typename T>
 __device__ __forceinline__ T ld(const T* p, long long q) { return __ldg(p + q); }
 
@@ -125,13 +137,13 @@ __device__ __forceinline__ T cell_residual(const Geom& g, const Coef<T>& c, cons
 // outside the interior copies its periodic image, rows j = 0..ny+1.  Used
 // once on fields that arrive from outside (the caller's fi).
 template <typename T>
-__global__ void k_ghost_xz(Geom g, T* __restrict__ p) {
+__device__ __forceinline__ void k_ghost_xz_blk(Geom g, T* __restrict__ p, const Blk& B) {
     const int nxg = g.nx + 2, nyg = g.ny + 2;
     const long long nplane = (long long)nxg * nyg;  // cells of one k = 0 / nz+1 plane
     const long long nside = 2LL * nyg * g.nz;       // i = 0 / nx+1 columns, k = 1..nz
     const long long tot = 2 * nplane + nside;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
-         t += (long long)gridDim.x * blockDim.x) {
+    for (long long t = B.x * (long long)blockDim.x + threadIdx.x; t < tot;
+         t += (long long)B.gx * blockDim.x) {
         int i, j, k;
         if (t < 2 * nplane) {
             int side = (int)(t / nplane);
@@ -151,6 +163,10 @@ __global__ void k_ghost_xz(Geom g, T* __restrict__ p) {
         int sk = k == 0 ? g.nz : (k == g.nz + 1 ? 1 : k);
         p[g.at(i, j, k)] = p[g.at(si, j, sk)];
     }
+}
+template <typename T>
+__global__ void k_ghost_xz(Geom g, T* __restrict__ p) {
+    k_ghost_xz_blk<T>(g, p, hw_blk());
 }
 
 // ---------------------------------------------------------------------------
@@ -349,19 +365,19 @@ __device__ __forceinline__ void relax_store(const Geom& g, const T* __restrict__
 // ZIN: pin is identically zero (first sweep of a correction); zk: pk is too.
 // Shared memory: 3 arrays [ny+2][32] and the segment maps [2][8][32].
 template <typename T, bool ZEBRA, bool ZIN>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
+__device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
-                                                    int kpar, int zk) {
+                                                    int kpar, int zk, const Blk& B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nj = g.ny + 2, ny = g.ny;
     T* G = reinterpret_cast<T*>(smem_raw);
     T* AL = G + nj * 32;
     T* CP = AL + nj * 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int k = ZEBRA ? 2 * blockIdx.x + 1 + kpar : blockIdx.x + 1;
+    const int k = ZEBRA ? 2 * B.x + 1 + kpar : B.x + 1;
     if (k > g.nz) return;
-    const int i = blockIdx.y * 32 + lane + 1;
+    const int i = B.y * 32 + lane + 1;
     const bool act = i <= g.nx;
     const bool odd = ZEBRA && (i & 1);  // updated in the second half
     const long long sj = g.sj, sk = g.sk;
@@ -454,17 +470,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_line_relax(Geom
         if (ZEBRA) __syncthreads();
     }
 }
+template <typename T, bool ZEBRA, bool ZIN>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
+                                                    const T* __restrict__ pin, const T* __restrict__ pk,
+                                                    T* __restrict__ pout, const T* __restrict__ rh, T omega,
+                                                    int kpar, int zk) {
+    k_line_relax_blk<T, ZEBRA, ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
+}
 
 // ---------------------------------------------------------------------------
 // Residual + restriction (resid_sndrcv.f03 followed by restrict_sndrcv.f03:
 // 32-53) for a coarsening ratio (rx,ry,rz) in {1,2}^3: coarse rh =
 // -(1/(rx*ry*rz)) * sum of the fine residuals L(p) - rh of its children.
 template <typename T>
-__global__ void k_resid_restrict(Geom gf, Geom gc, Coef<T> c, const T* __restrict__ p,
-                                 const T* __restrict__ rh, T* __restrict__ rhc, int rx, int ry, int rz) {
-    const int ic = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int jc = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int kc = blockIdx.z + 1;
+__device__ __forceinline__ void k_resid_restrict_blk(Geom gf, Geom gc, Coef<T> c, const T* __restrict__ p,
+                                 const T* __restrict__ rh, T* __restrict__ rhc, int rx, int ry, int rz, const Blk& B) {
+    const int ic = B.x * blockDim.x + threadIdx.x + 1;
+    const int jc = B.y * blockDim.y + threadIdx.y + 1;
+    const int kc = B.z + 1;
     if (ic > gc.nx || jc > gc.ny) return;
     T s = T(0);
     for (int dk = 0; dk < rz; ++dk)
@@ -473,26 +496,36 @@ __global__ void k_resid_restrict(Geom gf, Geom gc, Coef<T> c, const T* __restric
                 s += cell_residual(gf, c, p, rh, gf.at(rx * ic - di, ry * jc - dj, rz * kc - dk));
     rhc[gc.at(ic, jc, kc)] = -s / T(rx * ry * rz);
 }
+template <typename T>
+__global__ void k_resid_restrict(Geom gf, Geom gc, Coef<T> c, const T* __restrict__ p,
+                                 const T* __restrict__ rh, T* __restrict__ rhc, int rx, int ry, int rz) {
+    k_resid_restrict_blk<T>(gf, gc, c, p, rh, rhc, rx, ry, rz, hw_blk());
+}
 
 // Plain residual L(p) - rh into out (interior cells).
 template <typename T>
-__global__ void k_residual(Geom g, Coef<T> c, const T* __restrict__ p, const T* __restrict__ rh,
-                           T* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
+__device__ __forceinline__ void k_residual_blk(Geom g, Coef<T> c, const T* __restrict__ p, const T* __restrict__ rh,
+                           T* __restrict__ out, const Blk& B) {
+    const int i = B.x * blockDim.x + threadIdx.x + 1;
+    const int j = B.y * blockDim.y + threadIdx.y + 1;
+    const int k = B.z + 1;
     if (i > g.nx || j > g.ny) return;
     const long long q = g.at(i, j, k);
     out[q] = cell_residual(g, c, p, rh, q);
+}
+template <typename T>
+__global__ void k_residual(Geom g, Coef<T> c, const T* __restrict__ p, const T* __restrict__ rh,
+                           T* __restrict__ out) {
+    k_residual_blk<T>(g, c, p, rh, out, hw_blk());
 }
 
 // Restriction alone (restrict_sndrcv.f03:32-53), summed in the reference's
 // order for full coarsening.
 template <typename T>
-__global__ void k_restrict(Geom gf, Geom gc, const T* __restrict__ r, T* __restrict__ rc, int rx, int ry, int rz) {
-    const int ic = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int jc = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int kc = blockIdx.z + 1;
+__device__ __forceinline__ void k_restrict_blk(Geom gf, Geom gc, const T* __restrict__ r, T* __restrict__ rc, int rx, int ry, int rz, const Blk& B) {
+    const int ic = B.x * blockDim.x + threadIdx.x + 1;
+    const int jc = B.y * blockDim.y + threadIdx.y + 1;
+    const int kc = B.z + 1;
     if (ic > gc.nx || jc > gc.ny) return;
     const int id = rx * ic, jd = ry * jc, kd = rz * kc;
     T v;
@@ -509,6 +542,10 @@ __global__ void k_restrict(Geom gf, Geom gc, const T* __restrict__ r, T* __restr
             for (int di = 0; di < rx; ++di) v += r[gf.at(id - di, jd - dj, kd - dk)];
     rc[gc.at(ic, jc, kc)] = -v / T(rx * ry * rz);
 }
+template <typename T>
+__global__ void k_restrict(Geom gf, Geom gc, const T* __restrict__ r, T* __restrict__ rc, int rx, int ry, int rz) {
+    k_restrict_blk<T>(gf, gc, r, rc, rx, ry, rz, hw_blk());
+}
 
 // ---------------------------------------------------------------------------
 // Prolongation (prolong.f03:64-261): every fine cell, ghosts included, adds
@@ -517,11 +554,11 @@ __global__ void k_restrict(Geom gf, Geom gc, const T* __restrict__ r, T* __restr
 // 2c+1 gets (1/4, 3/4) -- the reference's (27/9/3/1)/64 weights for full
 // coarsening; along an uncoarsened direction the coarse value is copied.
 template <typename Tf, typename Tc>
-__global__ void k_prolong(Geom gf, Geom gc, Tf* __restrict__ pf, const Tc* __restrict__ pc, int rx, int ry,
-                          int rz) {
-    const int fi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int fj = blockIdx.y * blockDim.y + threadIdx.y;
-    const int fk = blockIdx.z;
+__device__ __forceinline__ void k_prolong_blk(Geom gf, Geom gc, Tf* __restrict__ pf, const Tc* __restrict__ pc, int rx, int ry,
+                          int rz, const Blk& B) {
+    const int fi = B.x * blockDim.x + threadIdx.x;
+    const int fj = B.y * blockDim.y + threadIdx.y;
+    const int fk = B.z;
     if (fi > gf.nx + 1 || fj > gf.ny + 1) return;
     int ci[2], cj[2], ck[2];
     Tc wi[2], wj[2], wk[2];
@@ -539,15 +576,20 @@ __global__ void k_prolong(Geom gf, Geom gc, Tf* __restrict__ pf, const Tc* __res
     const long long q = gf.at(fi, fj, fk);
     pf[q] = pf[q] + Tf(s);
 }
+template <typename Tf, typename Tc>
+__global__ void k_prolong(Geom gf, Geom gc, Tf* __restrict__ pf, const Tc* __restrict__ pc, int rx, int ry,
+                          int rz) {
+    k_prolong_blk<Tf, Tc>(gf, gc, pf, pc, rx, ry, rz, hw_blk());
+}
 
 // Prolongation for a level coarsened in x (rx = 2): one thread makes the
 // two fine cells 2c and 2c+1, which interpolate the same coarse pair
 // (c, c+1) with weights (3/4, 1/4) and (1/4, 3/4); y and z as in k_prolong.
 template <typename T>
-__global__ void k_prolong_x2(Geom gf, Geom gc, T* __restrict__ pf, const T* __restrict__ pc, int ry, int rz) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int fj = blockIdx.y * blockDim.y + threadIdx.y;
-    const int fk = blockIdx.z;
+__device__ __forceinline__ void k_prolong_x2_blk(Geom gf, Geom gc, T* __restrict__ pf, const T* __restrict__ pc, int ry, int rz, const Blk& B) {
+    const int c = B.x * blockDim.x + threadIdx.x;
+    const int fj = B.y * blockDim.y + threadIdx.y;
+    const int fk = B.z;
     if (c > gc.nx || fj > gf.ny + 1) return;
     const int cj = ry == 2 ? fj >> 1 : fj, ck = rz == 2 ? fk >> 1 : fk;
     const T wj0 = ry == 2 ? ((fj & 1) ? T(0.25) : T(0.75)) : T(1);
@@ -574,6 +616,10 @@ __global__ void k_prolong_x2(Geom gf, Geom gc, T* __restrict__ pf, const T* __re
     pf[qf] = pf[qf] + (T(0.75) * a + T(0.25) * bb);
     pf[qf + 1] = pf[qf + 1] + (T(0.25) * a + T(0.75) * bb);
 }
+template <typename T>
+__global__ void k_prolong_x2(Geom gf, Geom gc, T* __restrict__ pf, const T* __restrict__ pc, int ry, int rz) {
+    k_prolong_x2_blk<T>(gf, gc, pf, pc, ry, rz, hw_blk());
+}
 
 // ---------------------------------------------------------------------------
 // Exact solve on the coarsest level: e = S r with S the (pre-computed)
@@ -582,7 +628,7 @@ __global__ void k_prolong_x2(Geom gf, Geom gc, T* __restrict__ pf, const T* __re
 // = ((k-1)*nx + (i-1))*(ny+2) + j.  Each CTA stages r in shared memory; one
 // warp per row of S.
 template <typename T>
-__global__ void k_dense_solve(Geom g, const T* __restrict__ S, const T* __restrict__ rh, T* __restrict__ p) {
+__device__ __forceinline__ void k_dense_solve_blk(Geom g, const T* __restrict__ S, const T* __restrict__ rh, T* __restrict__ p, const Blk& B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* r = reinterpret_cast<T*>(smem_raw);
     const int nj = g.ny + 2;
@@ -594,7 +640,7 @@ __global__ void k_dense_solve(Geom g, const T* __restrict__ S, const T* __restri
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int u = B.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (u >= n) return;
     const T* row = S + (long long)u * n;
     T s = T(0);
@@ -604,6 +650,10 @@ __global__ void k_dense_solve(Geom g, const T* __restrict__ S, const T* __restri
         const int j = u % nj, col = u / nj;
         store_periodic(g, p, col % g.nx + 1, j, col / g.nx + 1, s);
     }
+}
+template <typename T>
+__global__ void k_dense_solve(Geom g, const T* __restrict__ S, const T* __restrict__ rh, T* __restrict__ p) {
+    k_dense_solve_blk<T>(g, S, rh, p, hw_blk());
 }
 
 }  // namespace ples

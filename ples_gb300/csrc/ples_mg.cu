@@ -24,16 +24,15 @@
 #include <vector>
 
 #include "line_tma.cuh"
+#include "handle.h"
 #include "mg_device.cuh"
+#include "outer_device.cuh"
 #include "metric.h"
 #include "ples_mg.h"
 
 using namespace ples;
 
 namespace {
-
-constexpr int kMaxLev = 12;
-constexpr int kRedThreads = 256;
 
 // ---------------------------------------------------------------------------
 // kernels of the outer loop, reductions and layout conversion
@@ -53,133 +52,15 @@ __global__ void k_scale_coef(long long n, const double* __restrict__ g11, const 
     }
 }
 
-__device__ __forceinline__ void block_reduce_sum_max(double& s, double& m) {
-    __shared__ double ss[32], sm[32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int o = 16; o; o >>= 1) {
-        s += __shfl_xor_sync(0xffffffffu, s, o);
-        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    }
-    if (lane == 0) { ss[w] = s; sm[w] = m; }
-    __syncthreads();
-    const int nw = (blockDim.x + 31) >> 5;
-    if (w == 0) {
-        s = lane < nw ? ss[lane] : 0.0;
-        m = lane < nw ? sm[lane] : 0.0;
-        for (int o = 16; o; o >>= 1) {
-            s += __shfl_xor_sync(0xffffffffu, s, o);
-            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        }
-    }
-}
-
-// r = b - L(x) on the fine level in FP64 (resid_sndrcv with the sign of the
-// inner right-hand side), stored in the inner precision; per-block partial
-// sum of squares and max |r| (multigrid.f03:595-631).
-template <typename Ti>
-__global__ void k_resid_outer(Geom g, Coef<double> c, const double* __restrict__ x, const double* __restrict__ b,
-                              Ti* __restrict__ rin, double* __restrict__ psq, double* __restrict__ pmax) {
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int i = blockIdx.x * 32 + tx + 1;
-    const int j = blockIdx.y * (kRedThreads / 32) + ty + 1;
-    const int k = blockIdx.z + 1;
-    double s = 0.0, m = 0.0;
-    if (i <= g.nx && j <= g.ny) {
-        const long long q = g.at(i, j, k);
-        const double r = -cell_residual(g, c, x, b, q);
-        rin[q] = Ti(r);
-        s = r * r;
-        m = fabs(r);
-    }
-    // NaN must survive the max: fmax drops NaN, so carry it in the sum
-    block_reduce_sum_max(s, m);
-    if (threadIdx.x == 0) {
-        const long long blk = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-        psq[blk] = s;
-        pmax[blk] = m;
-    }
-}
-
-// Face fluxes of the 19-point operator with the scaled coefficients (the
-// bracketed terms of res_dx / res_sop / res_av, resid_sndrcv.f03:85-147):
-// flux through csi-face i, eta-face j, zeta-face k of cell (i,j,k).
-__device__ __forceinline__ double flux_x(const Geom& g, const Coef<double>& c, const double* __restrict__ p,
-                                         long long q) {
-    const long long sj = g.sj, sk = g.sk;
-    return c.a1[q] * (p[q + 1] - p[q]) + c.b12[q] * (p[q + 1 + sj] + p[q + sj] - p[q + 1 - sj] - p[q - sj]) +
-           c.b13[q] * (p[q + 1 + sk] + p[q + sk] - p[q + 1 - sk] - p[q - sk]);
-}
-__device__ __forceinline__ double flux_y(const Geom& g, const Coef<double>& c, const double* __restrict__ p,
-                                         long long q) {
-    const long long sj = g.sj, sk = g.sk;
-    return c.a2[q] * (p[q + sj] - p[q]) + c.b21[q] * (p[q + 1 + sj] + p[q + 1] - p[q - 1 + sj] - p[q - 1]) +
-           c.b23[q] * (p[q + sj + sk] + p[q + sk] - p[q + sj - sk] - p[q - sk]);
-}
-__device__ __forceinline__ double flux_z(const Geom& g, const Coef<double>& c, const double* __restrict__ p,
-                                         long long q) {
-    const long long sj = g.sj, sk = g.sk;
-    return c.a3[q] * (p[q + sk] - p[q]) + c.b31[q] * (p[q + 1 + sk] + p[q + 1] - p[q - 1 + sk] - p[q - 1]) +
-           c.b32[q] * (p[q + sj + sk] + p[q + sj] - p[q - sj + sk] - p[q - sj]);
-}
-
-// r = b - L(x) with every face flux evaluated once and shared by its two
-// cells: the csi-face flux through the lane shuffle, the eta-face flux
-// through shared memory, the zeta-face flux carried while the thread walks
-// KC planes in k.  The FP64 pipe is the bound of this kernel, so sharing
-// roughly halves its time.  Per-block partial sum of squares and max |r|.
 template <typename Ti, int KC>
 __global__ void __launch_bounds__(256) k_resid_outer2(Geom g, Coef<double> c, const double* __restrict__ x,
                                                       const double* __restrict__ b, Ti* __restrict__ rin,
                                                       double* __restrict__ psq, double* __restrict__ pmax) {
-    __shared__ double sN[8][32];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int i = blockIdx.x * 32 + tx + 1, j = blockIdx.y * 8 + ty + 1;
-    const int k0 = blockIdx.z * KC + 1, k1 = min(k0 + KC - 1, g.nz);
-    const bool act = i <= g.nx && j <= g.ny;
-    const int ic = min(i, g.nx), jc = min(j, g.ny);  // keep idle threads' loads in the box
-    double s = 0.0, m = 0.0;
-    double fB = flux_z(g, c, x, g.at(ic, jc, k0 - 1));
-    for (int k = k0; k <= k1; ++k) {
-        const long long q = g.at(ic, jc, k);
-        const double fE = flux_x(g, c, x, q);
-        double fW = __shfl_up_sync(0xffffffffu, fE, 1);
-        if (tx == 0) fW = flux_x(g, c, x, q - 1);
-        const double fN = flux_y(g, c, x, q);
-        sN[ty][tx] = fN;
-        __syncthreads();
-        const double fS = ty > 0 ? sN[ty - 1][tx] : flux_y(g, c, x, q - g.sj);
-        __syncthreads();
-        const double fF = flux_z(g, c, x, q);
-        if (act) {
-            const double r = b[q] - ((fE - fW) + (fN - fS) + (fF - fB));
-            rin[q] = Ti(r);
-            s += r * r;
-            m = fmax(m, fabs(r));
-        }
-        fB = fF;
-    }
-    block_reduce_sum_max(s, m);
-    if (threadIdx.x == 0) {
-        const long long blk = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-        psq[blk] = s;
-        pmax[blk] = m;
-    }
+    k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk());
 }
 
-// sum / sum of squares of interior cells, per-block partials
 __global__ void k_sum_interior(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum) {
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int i = blockIdx.x * 32 + tx + 1;
-    const int j = blockIdx.y * (kRedThreads / 32) + ty + 1;
-    const int k = blockIdx.z + 1;
-    double s = 0.0, m = 0.0;
-    if (i <= g.nx && j <= g.ny) {
-        const double v = a[g.at(i, j, k)];
-        s = squares ? v * v : v;
-    }
-    block_reduce_sum_max(s, m);
-    if (threadIdx.x == 0)
-        psum[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s;
+    k_sum_interior_blk(g, a, squares, psum, hw_blk());
 }
 
 // deterministic final reduction of n partials (sum of a, max of bmax)
@@ -195,70 +76,25 @@ __global__ void k_reduce_final(const double* __restrict__ a, const double* __res
 }
 
 __global__ void k_add_interior(Geom g, double* __restrict__ a, double v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i <= g.nx && j <= g.ny) a[g.at(i, j, k)] += v;
+    k_add_interior_blk(g, a, v, hw_blk());
 }
 
 __global__ void k_add_box(Geom g, double* __restrict__ a, double v) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i <= g.nx + 1 && j <= g.ny + 1) a[g.at(i, j, k)] += v;
+    k_add_box_blk(g, a, v, hw_blk());
 }
 
 template <typename Te>
 __global__ void k_update(Geom g, double* __restrict__ x, const Te* __restrict__ e) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i <= g.nx + 1 && j <= g.ny + 1) {
-        const long long q = g.at(i, j, k);
-        x[q] += double(e[q]);
-    }
+    k_update_blk<Te>(g, x, e, hw_blk());
 }
 
-// FP64 wall ghost rows j = 0 and ny+1 from the current field
-// (mul_boun_sndrcv, multigrid.f03:1160-1186, freesurface = 0), written to a
-// side buffer so that one pass is a Jacobi step (race-free, deterministic).
 __global__ void k_wall_compute(Geom g, Coef<double> c, const double* __restrict__ p, double* __restrict__ w,
                                const double* __restrict__ cs3, const double* __restrict__ cs4, double an_dt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int k = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int side = blockIdx.z;
-    if (i > g.nx || k > g.nz) return;
-    const long long sj = g.sj, sk = g.sk;
-    const long long widx = (long long)side * g.nx * g.nz + (long long)(k - 1) * g.nx + (i - 1);
-    if (side == 0) {
-        const long long q0 = g.at(i, 0, k), q1 = q0 + sj;
-        const double a2 = c.a2[q0];
-        double v = p[q1];
-        if (cs3) v -= an_dt * cs3[(long long)(k - 1) * g.nx + (i - 1)] / a2;
-        v += (c.b21[q0] * (p[q1 + 1] + p[q0 + 1] - p[q1 - 1] - p[q0 - 1]) +
-              c.b23[q0] * (p[q1 + sk] + p[q0 + sk] - p[q1 - sk] - p[q0 - sk])) / a2;
-        w[widx] = v;
-    } else {
-        const long long qt = g.at(i, g.ny + 1, k), qn = qt - sj;
-        const double a2 = c.a2[qn];
-        double v = p[qn];
-        if (cs4) v += an_dt * cs4[(long long)(k - 1) * g.nx + (i - 1)] / a2;
-        v -= (c.b21[qn] * (p[qt + 1] + p[qn + 1] - p[qt - 1] - p[qn - 1]) +
-              c.b23[qn] * (p[qt + sk] + p[qn + sk] - p[qt - sk] - p[qn - sk])) / a2;
-        w[widx] = v;
-    }
+    k_wall_compute_blk(g, c, p, w, cs3, cs4, an_dt, hw_blk());
 }
 
-// scatter the wall rows, including their periodic x/z images (edges and
-// corners of the ghost shell)
 __global__ void k_wall_scatter(Geom g, double* __restrict__ p, const double* __restrict__ w) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = blockIdx.y * blockDim.y + threadIdx.y;
-    const int side = blockIdx.z;
-    if (i > g.nx + 1 || k > g.nz + 1) return;
-    const int wi = i == 0 ? g.nx : (i == g.nx + 1 ? 1 : i);
-    const int wk = k == 0 ? g.nz : (k == g.nz + 1 ? 1 : k);
-    p[g.at(i, side ? g.ny + 1 : 0, k)] = w[(long long)side * g.nx * g.nz + (long long)(wk - 1) * g.nx + (wi - 1)];
+    k_wall_scatter_blk(g, p, w, hw_blk());
 }
 
 // contraction factor of the Jacobi wall fill: max 2(|B21|+|B23|)/A2
@@ -272,26 +108,12 @@ __global__ void k_wall_contraction(Geom g, Coef<double> c, unsigned long long* o
     atomicMax(out, (unsigned long long)__double_as_longlong(v));
 }
 
-// compact Fortran arrays <-> ghosted boxes
 __global__ void k_compact_to_box(Geom g, int ghost, const double* __restrict__ src, double* __restrict__ dst) {
-    const int o = ghost ? 0 : 1;
-    const int ex = ghost ? g.nx + 2 : g.nx, ey = ghost ? g.ny + 2 : g.ny, ez = ghost ? g.nz + 2 : g.nz;
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    const int b = blockIdx.y * blockDim.y + threadIdx.y;
-    const int c = blockIdx.z;
-    if (a >= ex || b >= ey) return;
-    dst[g.at(a + o, b + o, c + o)] = src[((long long)c * ey + b) * ex + a];
-    (void)ez;
+    k_compact_to_box_blk(g, ghost, src, dst, hw_blk());
 }
 
 __global__ void k_box_to_compact(Geom g, int ghost, const double* __restrict__ src, double* __restrict__ dst) {
-    const int o = ghost ? 0 : 1;
-    const int ex = ghost ? g.nx + 2 : g.nx, ey = ghost ? g.ny + 2 : g.ny;
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    const int b = blockIdx.y * blockDim.y + threadIdx.y;
-    const int c = blockIdx.z;
-    if (a >= ex || b >= ey) return;
-    dst[((long long)c * ey + b) * ex + a] = src[g.at(a + o, b + o, c + o)];
+    k_box_to_compact_blk(g, ghost, src, dst, hw_blk());
 }
 
 // face arrays with the reference extents: (i0:i1, j0:j1, k0:k1) of a box
@@ -320,82 +142,7 @@ inline int grid1(long long n, int t = 256) {
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-struct LevelData {
-    Geom g;
-    int rx = 1, ry = 1, rz = 1;  // coarsening ratio from the finer level
-    int sx = 1, sy = 1, sz = 1;  // cumulative node strides relative to level 1
-    double inv_div = 1.0;        // raw metric = t * inv_div
-    double post = 1.0;           // stored coefficient = raw * post (x 1/4 on cross terms)
-    void* p = nullptr;           // inner-precision fields (T boxes)
-    void* p2 = nullptr;
-    void* rh = nullptr;
-    void* cp = nullptr;          // LU factor c' of the eta-line operator (T box)
-    Coef<float> cf{};             // FP32 scaled coefficients (mixed)
-    Coef<double> cd{};            // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
-    bool has_cf = false, has_cd = false;
-    // TMA-staged zebra smoother (FP32): tensor maps of this level's fields;
-    // pA/pB are the buffers behind maps.pA/pB (p and p2 swap every sweep)
-    bool tma = false;
-    void *pA = nullptr, *pB = nullptr;
-    LineMaps maps{};
-};
-
-struct ples_mg_handle {
-    ples_mg_desc d{};
-    int dev = 0;
-    cudaStream_t st = nullptr;
-    int nlev = 0;
-    LevelData L[kMaxLev];
-    double *xn = nullptr, *yn = nullptr, *zn = nullptr;  // fine nodes (0:jx,0:jy,0:jz)
-    double *x = nullptr, *b = nullptr;                   // FP64 solution / rhs boxes (level 1)
-    double* wbuf = nullptr;                              // 2*nx*nz wall rows
-    double *part_a = nullptr, *part_b = nullptr;         // block partials
-    long long npart = 0;
-    double* red = nullptr;                               // 2 doubles on the device (+ dflag)
-    int* dflag = nullptr;                                // bounded-wait error flag, inside red
-    double* h_red = nullptr;                             // pinned host copy
-    double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
-    double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes
-    double* cs_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // their device buffers
-    void* coarse_S = nullptr;                            // dense inverse of the coarsest system (T)
-    int coarse_n = 0;
-    int wall_passes = 3;
-    double wall_q = 0.0;
-    int nu_pre = 2, nu_post = 2, nu_coarse = 40, inner_cycles = 3, smoother = 0;
-    double omega = 0.8;
-    std::vector<void*> allocs;
-    std::string err;
-    long long bytes = 0;
-    // instrumentation: kernels launched, and optional CUDA-event timing of
-    // one kernel kind at one level (pairs are read back after each solve)
-    long long launches = 0;
-    int timed_kind = -1, timed_level = 0;
-    std::vector<cudaEvent_t> ev_pool;
-    size_t ev_used = 0;
-    double timed_ms = 0.0;
-    long long timed_launches = 0;
-};
-
 namespace {
-
-int fail(ples_mg_handle* h, int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof buf, fmt, ap);
-    va_end(ap);
-    if (h) h->err = buf;
-    return code;
-}
-
-#define CK(call)                                                                               \
-    do {                                                                                       \
-        cudaError_t e_ = (call);                                                               \
-        if (e_ != cudaSuccess)                                                                 \
-            return fail(h, e_ == cudaErrorMemoryAllocation ? PLES_MG_OOM : PLES_MG_CUDA_ERROR, \
-                        "%s failed: %s", #call, cudaGetErrorString(e_));                       \
-    } while (0)
 
 // kernel kinds for the optional event timing
 enum { KIND_LINE = 0, KIND_RESTRICT = 1, KIND_PROLONG = 2, KIND_OUTER = 3, KIND_COARSE = 4, KIND_WALL = 5 };

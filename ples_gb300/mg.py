@@ -60,7 +60,10 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_strerror", "ples_mg_last_error", "ples_mg_levels", "ples_mg_level_dims",
            "ples_mg_get_metric", "ples_mg_apply_residual", "ples_mg_apply_ghost_fill",
            "ples_mg_apply_restrict", "ples_mg_apply_prolong", "ples_mg_counters",
-           "ples_mg_kernel_timing", "ples_mg_kernel_time", "ples_mg_residual_norms_device")
+           "ples_mg_kernel_timing", "ples_mg_kernel_time", "ples_mg_batch_create",
+           "ples_mg_batch_solve", "ples_mg_batch_solve_device", "ples_mg_batch_info",
+           "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
+           "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_residual_norms_device")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -95,6 +98,21 @@ def load(build=True):
     L.ples_mg_kernel_timing.argtypes = [vp, C.c_int, C.c_int]
     L.ples_mg_kernel_time.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.ples_mg_residual_norms_device.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_double)]
+    L.ples_mg_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
+    L.ples_mg_batch_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
+    L.ples_mg_batch_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
+    L.ples_mg_batch_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+    L.ples_mg_batch_last_error.argtypes = [vp]
+    L.ples_mg_batch_last_error.restype = C.c_char_p
+    L.ples_mg_batch_destroy.argtypes = [vp]
+    L.ples_mg_batch_destroy.restype = None
+    L.ples_srv_create.argtypes = [vp, C.c_int, C.c_double, C.POINTER(vp)]
+    L.ples_srv_submit.argtypes = [vp, C.c_int, vp, vp, C.c_double, C.c_int, C.POINTER(C.c_longlong)]
+    L.ples_srv_wait.argtypes = [vp, C.c_longlong, C.POINTER(Stats)]
+    L.ples_srv_report.argtypes = [vp] + [C.POINTER(C.c_double)] * 3 + [C.POINTER(C.c_longlong),
+                                                                       C.POINTER(C.c_double)]
+    L.ples_srv_destroy.argtypes = [vp]
+    L.ples_srv_destroy.restype = None
     _lib = L
     return L
 
@@ -276,3 +294,142 @@ class Multigrid:
         prf = _f64(prf).copy(order="F")
         self._check(self._L.ples_mg_apply_prolong(self._h, level, prf, _f64(prc)))
         return prf
+
+
+def _ptr_array(ptrs):
+    arr = (C.c_void_p * len(ptrs))(*[None if p is None else int(p) for p in ptrs])
+    return arr
+
+
+class Batch:
+    """Many grids solved together (ples_mg_batch_*): the members are
+    Multigrid objects (mixed precision, zebra smoother, full coarsening)
+    that keep their resident hierarchies."""
+
+    def __init__(self, members):
+        self._L = load()
+        self.members = list(members)
+        hs = (C.c_void_p * len(self.members))(*[m._h.value for m in self.members])
+        b = C.c_void_p()
+        rc = self._L.ples_mg_batch_create(C.cast(hs, C.c_void_p), len(self.members), C.byref(b))
+        if rc != OK:
+            raise PlesMGError(rc, self._L.ples_mg_strerror(rc).decode())
+        self._b = b
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._L.ples_mg_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, allow=(OK, NOT_CONVERGED)):
+        if rc not in allow:
+            raise PlesMGError(rc, f"{self._L.ples_mg_strerror(rc).decode()}: "
+                                  f"{self._L.ples_mg_batch_last_error(self._b).decode()}")
+        return rc
+
+    def solve(self, rhs_list, fi_list=None, rel_tol=1e-10, max_cycles=200):
+        """Host arrays; returns (list of fi, list of stats dicts).  fi_list
+        None starts every member from zero."""
+        n = len(self.members)
+        if fi_list is None:
+            fi_list = [np.zeros((m.jx + 2, m.jy + 2, m.jz + 2), order="F") for m in self.members]
+        fis = [_f64(f).copy(order="F") for f in fi_list]
+        rhs = [_f64(r) for r in rhs_list]
+        for m, f, r in zip(self.members, fis, rhs, strict=True):
+            if f.shape != (m.jx + 2, m.jy + 2, m.jz + 2) or r.shape != (m.jx, m.jy, m.jz):
+                raise ValueError("fi/rhs shapes must match the members' grids")
+        st = (Stats * n)()
+        rc = self._L.ples_mg_batch_solve(self._b, C.cast(_ptr_array([f.ctypes.data for f in fis]), C.c_void_p),
+                                         C.cast(_ptr_array([r.ctypes.data for r in rhs]), C.c_void_p),
+                                         rel_tol, max_cycles, C.cast(st, C.c_void_p))
+        self._check(rc)
+        return fis, [s.as_dict() for s in st]
+
+    def solve_device(self, d_fi, d_rhs, rel_tol=1e-10, max_cycles=200):
+        """Device buffers (integer pointers) in the Fortran layouts."""
+        n = len(self.members)
+        st = (Stats * n)()
+        rc = self._L.ples_mg_batch_solve_device(self._b, C.cast(_ptr_array(d_fi), C.c_void_p),
+                                                C.cast(_ptr_array(d_rhs), C.c_void_p), rel_tol, max_cycles,
+                                                C.cast(st, C.c_void_p))
+        self._check(rc)
+        return [s.as_dict() for s in st]
+
+    def info(self):
+        s, r = C.c_int(), C.c_longlong()
+        self._L.ples_mg_batch_info(self._b, C.byref(s), C.byref(r))
+        return {"steps": s.value, "replays": r.value}
+
+
+class Server:
+    """Request server with continuous batching (ples_srv_*)."""
+
+    def __init__(self, members, hbm_budget_bytes=0.0):
+        self._L = load()
+        self.members = list(members)
+        hs = (C.c_void_p * len(self.members))(*[m._h.value for m in self.members])
+        s = C.c_void_p()
+        rc = self._L.ples_srv_create(C.cast(hs, C.c_void_p), len(self.members), hbm_budget_bytes, C.byref(s))
+        if rc != OK:
+            raise PlesMGError(rc, self._L.ples_mg_strerror(rc).decode())
+        self._s = s
+        self._out = {}
+
+    def close(self):
+        if getattr(self, "_s", None):
+            self._L.ples_srv_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, member, rhs, rel_tol=1e-10, max_cycles=200):
+        m = self.members[member]
+        out = np.zeros((m.jx + 2, m.jy + 2, m.jz + 2), order="F")
+        r = _f64(rhs)  # held until the call returns: the server copies it
+        if r.shape != (m.jx, m.jy, m.jz):
+            raise ValueError(f"rhs of member {member} must be {(m.jx, m.jy, m.jz)}")
+        t = C.c_longlong()
+        rc = self._L.ples_srv_submit(self._s, member, C.c_void_p(r.ctypes.data),
+                                     C.c_void_p(out.ctypes.data), rel_tol, max_cycles, C.byref(t))
+        if rc != OK:
+            raise PlesMGError(rc, self._L.ples_mg_strerror(rc).decode())
+        self._out[t.value] = out
+        return t.value
+
+    def wait(self, ticket):
+        """Returns (fi, stats dict); stats['seconds'] is the request latency."""
+        st = Stats()
+        rc = self._L.ples_srv_wait(self._s, ticket, C.byref(st))
+        out = self._out.pop(ticket, None)
+        if rc not in (OK, NOT_CONVERGED):
+            raise PlesMGError(rc, self._L.ples_mg_strerror(rc).decode())
+        return out, st.as_dict()
+
+    def report(self):
+        a, b, c, sps = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        n = C.c_longlong()
+        self._L.ples_srv_report(self._s, C.byref(a), C.byref(b), C.byref(c), C.byref(n), C.byref(sps))
+        return {"p50_ms": a.value, "p99_ms": b.value, "p999_ms": c.value, "completed": n.value,
+                "solves_per_s": sps.value}

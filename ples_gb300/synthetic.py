@@ -33,6 +33,12 @@ __all__ = [
     "write_gri3dp",
     "Workload",
     "WORKLOADS",
+    "BATCH_SIZES",
+    "batch_instances",
+    "SERVE_SIZES",
+    "serve_members",
+    "poisson_arrivals",
+    "next_rhs",
 ]
 
 
@@ -129,3 +135,52 @@ WORKLOADS = {
     "channel_256x128x256": Workload("channel_256x128x256", 256, 128, 256, 0.1, 2.5, 1),
     "channel_512x256x512": Workload("channel_512x256x512", 512, 256, 512, 0.1, 3.0, 4),
 }
+
+# Many-grid workloads.  Batched solves: 64 independent instances, seeds
+# 2..65; each seed draws its grid size uniformly from BATCH_SIZES, then the
+# wall amplitude A ~ U(0, 0.15) and the stretch beta ~ U(1.5, 3.0), with
+# numpy.random.default_rng(seed); the RHS is divergence_rhs(..., seed).
+BATCH_SIZES = ((32, 32, 32), (48, 32, 48), (64, 64, 64), (96, 48, 96), (128, 64, 128))
+
+
+def batch_instances(seeds=range(2, 66)):
+    """Workloads of the batched-solve case, one per seed."""
+    out = []
+    for seed in seeds:
+        rng = np.random.default_rng(seed)
+        jx, jy, jz = BATCH_SIZES[int(rng.integers(len(BATCH_SIZES)))]
+        amp, beta = float(rng.uniform(0.0, 0.15)), float(rng.uniform(1.5, 3.0))
+        out.append(Workload(f"batch_{seed}", jx, jy, jz, amp, beta, seed))
+    return out
+
+
+# Served ensemble: 16 members, member m drawing its fixed grid from
+# SERVE_SIZES and A, beta as above with default_rng(1000 + m); its first RHS
+# uses seed 1000 + m, every later one is the previous plus 5% N(0,1) noise
+# (re-mean-zeroed), and each solve warm-starts from the member's previous
+# solution.
+SERVE_SIZES = ((48, 48, 48), (96, 48, 96), (128, 64, 128), (192, 96, 192))
+
+
+def serve_members(n=16):
+    out = []
+    for m in range(n):
+        rng = np.random.default_rng(1000 + m)
+        jx, jy, jz = SERVE_SIZES[int(rng.integers(len(SERVE_SIZES)))]
+        amp, beta = float(rng.uniform(0.0, 0.15)), float(rng.uniform(1.5, 3.0))
+        out.append(Workload(f"member_{m}", jx, jy, jz, amp, beta, 1000 + m))
+    return out
+
+
+def poisson_arrivals(rate, n, seed=7, members=16):
+    """n arrival times (s, from 0) of a Poisson process with the given
+    aggregate rate, each for a member drawn uniformly."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    return t - t[0], rng.integers(members, size=n)
+
+
+def next_rhs(rhs, rng, frac=0.05):
+    """The next time step's right-hand side of a member."""
+    r = rhs + frac * rng.standard_normal(rhs.shape)
+    return np.asfortranarray(r - r.mean())

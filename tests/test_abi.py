@@ -16,7 +16,7 @@ HDR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 
 def declared_functions():
     txt = open(HDR).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(ples_mg_\w+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(ples_(?:mg|srv)_\w+)\s*\(", txt)))
 
 
 def test_library_builds_and_loads():

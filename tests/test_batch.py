@@ -1,0 +1,134 @@
+"""Batched solves and the request server, through the C ABI.
+
+Tolerances: every member converged to ||r||/||b|| <= 1e-10; zero-mean
+solutions within 1e-8 (L2 and max, relative) of the oracle's converged
+solution, and within 1e-9 of the same grid solved alone by ples_mg_solve
+(same kernels; only the reduction order of the compatibility shift
+differs).  A request's result is the same alone and in a mix of concurrent
+requests (each member's arithmetic is independent of the others): within
+1e-12.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from ples_gb300 import mg
+from ples_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-10
+
+
+def _zm(fi):
+    p = fi[1:-1, 1:-1, 1:-1]
+    return p - p.mean()
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b), np.abs(a - b).max() / np.abs(b).max()
+
+
+# uneven sizes and depths (coarsest 3x2x3 .. 4x2x4, 4 to 6 levels)
+SIZES = [(32, 16, 32), (48, 32, 48), (24, 16, 24), (64, 32, 64), (32, 32, 32)]
+
+
+def _case(dims, seed):
+    rng = np.random.default_rng(seed)
+    amp, beta = rng.uniform(0.0, 0.15), rng.uniform(1.5, 3.0)
+    x, y, z = S.wavy_channel_grid(*dims, amp, beta)
+    return x, y, z, S.divergence_rhs(*dims, seed=seed)
+
+
+@pytest.fixture(scope="module")
+def cases():
+    return [_case(d, 100 + i) for i, d in enumerate(SIZES)]
+
+
+def test_batch_matches_single_solves_and_oracle(cases):
+    members = [mg.Multigrid(x, y, z) for x, y, z, _ in cases]
+    rhs = [c[3] for c in cases]
+    with mg.Batch(members) as b:
+        fis, sts = b.solve(rhs, rel_tol=REL_TOL)
+        info = b.info()
+        assert info["steps"] > 50
+        # again, from zero: identical (the same graph, deterministic)
+        fis2, sts2 = b.solve(rhs, rel_tol=REL_TOL)
+    for i, (fi, st) in enumerate(zip(fis, sts)):
+        assert st["status"] == mg.OK and st["rel_residual"] <= REL_TOL, (i, st)
+        np.testing.assert_array_equal(fi, fis2[i])
+        assert sts2[i]["outer_iterations"] == st["outer_iterations"]
+        fo, so = members[i].solve(rhs[i], rel_tol=REL_TOL)
+        l2, mx = _rel(_zm(fi), _zm(fo))
+        assert l2 <= 1e-9 and mx <= 1e-9, (i, l2, mx)
+        assert abs(st["outer_iterations"] - so["outer_iterations"]) <= 1
+    # the oracle on the smallest member
+    x, y, z, r = cases[2]
+    ref, *_ = Oracle(x, y, z, islor=1).multi(r, eps=1e-13, ficycle=400)
+    l2, mx = _rel(_zm(fis[2]), _zm(ref))
+    assert l2 <= 1e-8 and mx <= 1e-8
+    for m in members:
+        m.close()
+
+
+def test_batch_rejects_unsupported_members(cases):
+    x, y, z, _ = cases[0]
+    with mg.Multigrid(x, y, z, precision="fp64") as m:
+        with pytest.raises(mg.PlesMGError):
+            mg.Batch([m])
+
+
+def test_server_same_result_alone_and_in_the_mix(cases):
+    # identical grids on separate handles, both starting from zero
+    alone = [mg.Multigrid(*cases[1][:3])]
+    mix = [mg.Multigrid(*c[:3]) for c in cases[:4]]
+    with mg.Server(alone) as s:
+        r1, st1 = s.wait(s.submit(0, cases[1][3], rel_tol=REL_TOL))
+    assert st1["status"] == mg.OK and st1["rel_residual"] <= REL_TOL
+    with mg.Server(mix, hbm_budget_bytes=150e9) as s:
+        tickets = {}
+        lock = threading.Lock()
+
+        def client(i):
+            t = s.submit(i, cases[i][3], rel_tol=REL_TOL)
+            with lock:
+                tickets[i] = t
+
+        th = [threading.Thread(target=client, args=(i,)) for i in (0, 2, 3, 1)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        res = {i: s.wait(tickets[i]) for i in tickets}
+        rep = s.report()
+    r2, st2 = res[1]
+    assert st2["status"] == mg.OK
+    assert np.abs(r2 - r1).max() <= 1e-12 * np.abs(r1).max()
+    assert st2["outer_iterations"] == st1["outer_iterations"]
+    assert rep["completed"] == 4 and rep["p99_ms"] >= rep["p50_ms"] > 0.0
+    for i, (fi, st) in res.items():
+        assert st["status"] == mg.OK and st["rel_residual"] <= REL_TOL
+    for m in alone + mix:
+        m.close()
+
+
+def test_server_warm_start_and_budget(cases):
+    x, y, z, rhs = cases[0]
+    with mg.Multigrid(x, y, z) as m:
+        with pytest.raises(mg.PlesMGError):
+            mg.Server([m], hbm_budget_bytes=1e3)
+        with mg.Server([m]) as s:
+            _, cold = s.wait(s.submit(0, rhs, rel_tol=REL_TOL))
+            rng = np.random.default_rng(5)
+            # a small change of the right-hand side: the warm start begins
+            # some eight decades closer to the new solution
+            rhs2 = rhs + 1e-8 * rng.standard_normal(rhs.shape)
+            rhs2 -= rhs2.mean()
+            fi, warm = s.wait(s.submit(0, rhs2, rel_tol=REL_TOL))
+        assert warm["status"] == mg.OK
+        assert warm["outer_iterations"] < cold["outer_iterations"]
+        fo, _ = m.solve(rhs2, rel_tol=REL_TOL)
+        l2, mx = _rel(_zm(fi), _zm(fo))
+        assert l2 <= 1e-8 and mx <= 1e-8
