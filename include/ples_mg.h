@@ -150,6 +150,24 @@ int ples_mg_counters(ples_mg_handle *h, long long *launches, long long *device_b
 int ples_mg_kernel_timing(ples_mg_handle *h, int kind, int level);
 int ples_mg_kernel_time(ples_mg_handle *h, double *total_ms, long long *launches);
 
+/* ---- autotuner ----------------------------------------------------------
+ * No counterpart in the reference (its kss, nlevel and omega are fixed
+ * inputs).  Times candidate settings on this handle's grid and keeps the
+ * fastest: the CTA width of the eta-line smoother per level (128 or 256
+ * threads, by kernel time) and then the sweeps per level (nu_pre = nu_post
+ * in 1..3) and V-cycles per outer iteration (2, 3, 4, 6), by the time of a
+ * whole solve to ||r||/||b|| <= 1e-10 from zero.  rhs (host, (1:jx,1:jy,
+ * 1:jz)) or NULL for a pseudo-random compatible one.  Batches created
+ * afterwards use the tuned settings of their members. */
+typedef struct {
+    int nu;               /* sweeps per level before and after the coarse correction */
+    int inner_cycles;     /* V-cycles per FP64 outer iteration */
+    int line_threads[12]; /* smoother CTA width per level (0 past the last level) */
+    double solve_ms;      /* one solve with the chosen setting */
+    int candidates;       /* settings timed */
+} ples_mg_tuning;
+int ples_mg_autotune(ples_mg_handle *h, const double *rhs, ples_mg_tuning *out);
+
 /* ---- many grids at once ------------------------------------------------
  * No counterpart in the reference, which solves one grid per run.  A batch
  * groups existing handles (mixed precision, zebra smoother, full

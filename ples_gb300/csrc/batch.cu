@@ -246,8 +246,8 @@ enum Kind { K_GHOST, K_SUM, K_RED, K_ADD, K_WALLC, K_WALLS, K_ROUT, K_LINE0, K_L
 struct Step {
     int kind, phase;
     int ntask = 0, total = 0;
-    size_t off = 0;  // byte offset of the task array in the table buffer
-    int grid = 0;
+    size_t off = 0;    // byte offset of the task array in the table buffer
+    int threads = 0;   // CTA width of a smoother step (the tuned width of its largest grid)
 };
 
 }  // namespace
@@ -399,6 +399,7 @@ int build_steps(ples_mg_batch* b) {
     auto line_steps = [&](int c, int n, int s, bool zin) {  // one sweep of level n for the members in it
         for (int par = 0; par < 2; ++par) {
             B.begin<LineTask>(zin ? K_LINE1 : K_LINE0, PH_ITER);
+            long long big = -1;
             for (int i = 0; i < nm; ++i) {
                 ples_mg_handle* h = b->mem[i];
                 if (c >= h->inner_cycles || n > h->nlev - 2 || s >= h->nu_pre) continue;
@@ -416,6 +417,11 @@ int build_steps(ples_mg_batch* b) {
                 t.kpar = par;
                 t.zk = (zin && par == 0) ? 1 : 0;
                 B.add(t, line_grid(L.g));
+                const long long cells = (long long)L.g.nx * L.g.ny * L.g.nz;
+                if (cells > big) {
+                    big = cells;
+                    B.cur.threads = L.line_threads;
+                }
             }
             B.end();
         }
@@ -615,8 +621,12 @@ int record_steps(ples_mg_batch* b) {
             case K_WALLC: rc = launch_step<WallCTask>(b, s, i, kb_wallc<WallCTask>, b2, 0); break;
             case K_WALLS: rc = launch_step<WallSTask>(b, s, i, kb_walls<WallSTask>, b2, 0); break;
             case K_ROUT: rc = launch_step<RoutTask>(b, s, i, kb_rout<RoutTask>, b1, 0); break;
-            case K_LINE0: rc = launch_step<LineTask>(b, s, i, kb_line<LineTask, false>, b1, b->smem_line); break;
-            case K_LINE1: rc = launch_step<LineTask>(b, s, i, kb_line<LineTask, true>, b1, b->smem_line); break;
+            case K_LINE0:
+                rc = launch_step<LineTask>(b, s, i, kb_line<LineTask, false>, dim3(s.threads), b->smem_line);
+                break;
+            case K_LINE1:
+                rc = launch_step<LineTask>(b, s, i, kb_line<LineTask, true>, dim3(s.threads), b->smem_line);
+                break;
             case K_RR: rc = launch_step<RRTask>(b, s, i, kb_rr<RRTask>, b2, 0); break;
             case K_DENSE: rc = launch_step<DenseTask>(b, s, i, kb_dense<DenseTask>, b1, b->smem_dense); break;
             case K_PROL: rc = launch_step<ProlTask>(b, s, i, kb_prol<ProlTask>, b2, 0); break;

@@ -367,19 +367,19 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
         } else if (h->smoother != 1) {  // zebra: two launches, k parities
             dim3 grd((L.g.nz + 1) / 2, (L.g.nx + 31) / 32);
             if (zin) {
-                k_line_relax<T, true, true><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
-                k_line_relax<T, true, true><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
+                k_line_relax<T, true, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
+                k_line_relax<T, true, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
             } else {
-                k_line_relax<T, true, false><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
-                k_line_relax<T, true, false><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
+                k_line_relax<T, true, false><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
+                k_line_relax<T, true, false><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
             }
             h->launches += 2;
         } else {  // Jacobi over lines
             dim3 grd(L.g.nz, (L.g.nx + 31) / 32);
             if (zin)
-                k_line_relax<T, false, true><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
+                k_line_relax<T, false, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
             else
-                k_line_relax<T, false, false><<<grd, 256, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
+                k_line_relax<T, false, false><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
             ++h->launches;
         }
         timed_end(h, KIND_LINE, level);
@@ -1295,6 +1295,110 @@ int ples_mg_kernel_time(ples_mg_handle* h, double* total_ms, long long* launches
     if (total_ms) *total_ms = h->timed_ms;
     if (launches) *launches = h->timed_launches;
     return PLES_MG_OK;
+}
+
+// Autotuner: first the CTA width of the eta-line smoother per level (128 or
+// 256 threads; the kernel's own time, CUDA events), then the sweep count per
+// level and the V-cycles per outer iteration (time of whole solves to
+// ||r||/||b|| <= 1e-10 from zero).  The fastest setting is kept in the handle.
+int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) {
+    if (!h || !out) return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        const Geom& g = h->L[0].g;
+        const size_t nrh = (size_t)g.nx * g.ny * g.nz;
+        std::vector<double> gen;
+        const double* src = rhs;
+        if (!src) {  // a compatible pseudo-random right-hand side (xorshift64)
+            gen.resize(nrh);
+            unsigned long long st = 0x9E3779B97F4A7C15ull;
+            double mean = 0.0;
+            for (auto& v : gen) {
+                st ^= st << 13;
+                st ^= st >> 7;
+                st ^= st << 17;
+                v = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+                mean += v;
+            }
+            mean /= (double)nrh;
+            for (auto& v : gen) v -= mean;
+            src = gen.data();
+        }
+        CK(cudaMemcpyAsync(h->rhs_c, src, 8 * nrh, cudaMemcpyHostToDevice, h->st));
+        struct Ev {
+            cudaEvent_t a = nullptr, b = nullptr;
+            ~Ev() {
+                if (a) cudaEventDestroy(a);
+                if (b) cudaEventDestroy(b);
+            }
+        } ev;
+        CK(cudaEventCreate(&ev.a));
+        CK(cudaEventCreate(&ev.b));
+        for (int c = 0; c < 6; ++c) h->cs_c[c] = nullptr;
+        auto trial = [&](int reps, double* ms, ples_mg_stats* st) -> int {
+            double tot = 0.0;
+            for (int q = 0; q < reps; ++q) {
+                k_compact_to_box<<<compact_grid(g, 0), dim3(32, 4), 0, h->st>>>(g, 0, h->rhs_c, h->b);
+                CK(cudaMemsetAsync(h->x, 0, 8 * (size_t)g.n, h->st));
+                CK(cudaEventRecord(ev.a, h->st));
+                *st = ples_mg_stats{};
+                const int rc = solve_any(h, 1e-10, 0.0, 200, st);
+                if (rc != PLES_MG_OK && rc != PLES_MG_NOT_CONVERGED) return rc;
+                CK(cudaEventRecord(ev.b, h->st));
+                CK(cudaEventSynchronize(ev.b));
+                float f = 0.f;
+                CK(cudaEventElapsedTime(&f, ev.a, ev.b));
+                tot += f;
+            }
+            *ms = tot / reps;
+            return PLES_MG_OK;
+        };
+        int rc, tried = 0;
+        double ms;
+        ples_mg_stats st;
+        const int nsmooth = h->coarse_S ? h->nlev - 1 : h->nlev;
+        for (int n = 0; n < nsmooth; ++n) {
+            double best = 1e300;
+            int bt = h->L[n].line_threads;
+            for (int t : {128, 256}) {
+                h->L[n].line_threads = t;
+                ples_mg_kernel_timing(h, KIND_LINE, n + 1);
+                if ((rc = trial(1, &ms, &st))) return rc;
+                double kms = 0.0;
+                long long kn = 0;
+                ples_mg_kernel_time(h, &kms, &kn);
+                ++tried;
+                if (kn > 0 && kms / kn < best) {
+                    best = kms / kn;
+                    bt = t;
+                }
+            }
+            h->L[n].line_threads = bt;
+        }
+        ples_mg_kernel_timing(h, -1, 0);
+        int bnu = h->nu_pre, bin = h->inner_cycles;
+        double bms = 1e300;
+        for (int nu : {1, 2, 3})
+            for (int inner : {2, 3, 4, 6}) {
+                h->nu_pre = h->nu_post = nu;
+                h->inner_cycles = inner;
+                if ((rc = trial(1, &ms, &st)) || (rc = trial(2, &ms, &st))) return rc;
+                ++tried;
+                if (st.status == PLES_MG_OK && ms < bms) {
+                    bms = ms;
+                    bnu = nu;
+                    bin = inner;
+                }
+            }
+        h->nu_pre = h->nu_post = bnu;
+        h->inner_cycles = bin;
+        std::memset(out, 0, sizeof *out);
+        out->nu = bnu;
+        out->inner_cycles = bin;
+        for (int n = 0; n < h->nlev && n < 12; ++n) out->line_threads[n] = h->L[n].line_threads;
+        out->solve_ms = bms;
+        out->candidates = tried;
+        return bms < 1e300 ? PLES_MG_OK : fail(h, PLES_MG_NOT_CONVERGED, "no candidate converged");
+    });
 }
 
 }  // extern "C"

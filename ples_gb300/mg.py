@@ -43,6 +43,11 @@ class Desc(C.Structure):
                 ("inner_cycles", C.c_int), ("smoother", C.c_int), ("coarsening", C.c_int)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("nu", C.c_int), ("inner_cycles", C.c_int), ("line_threads", C.c_int * 12),
+                ("solve_ms", C.c_double), ("candidates", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("outer_iterations", C.c_int), ("vcycles", C.c_int),
                 ("rel_residual", C.c_double), ("max_residual", C.c_double),
@@ -63,7 +68,8 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_kernel_timing", "ples_mg_kernel_time", "ples_mg_batch_create",
            "ples_mg_batch_solve", "ples_mg_batch_solve_device", "ples_mg_batch_info",
            "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
-           "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_residual_norms_device")
+           "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune",
+           "ples_mg_residual_norms_device")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -98,6 +104,7 @@ def load(build=True):
     L.ples_mg_kernel_timing.argtypes = [vp, C.c_int, C.c_int]
     L.ples_mg_kernel_time.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.ples_mg_residual_norms_device.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_double)]
+    L.ples_mg_autotune.argtypes = [vp, vp, C.POINTER(Tuning)]
     L.ples_mg_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
     L.ples_mg_batch_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
     L.ples_mg_batch_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
@@ -244,6 +251,17 @@ class Multigrid:
             self._h, C.c_void_p(int(d_fi)), C.c_void_p(int(d_rhs)), C.c_void_p(int(d_r) or None),
             C.c_void_p(int(stream) or None), out))
         return out[0], out[1]
+
+    def autotune(self, rhs=None):
+        """Time candidate smoother widths, sweep counts and inner cycles on
+        this grid and keep the fastest (ples_mg_autotune)."""
+        t = Tuning()
+        keep = None if rhs is None else _f64(rhs)
+        ptr = None if keep is None else C.c_void_p(keep.ctypes.data)
+        self._check(self._L.ples_mg_autotune(self._h, ptr, C.byref(t)))
+        return {"nu": t.nu, "inner_cycles": t.inner_cycles,
+                "line_threads": [v for v in t.line_threads if v], "solve_ms": t.solve_ms,
+                "candidates": t.candidates}
 
     # -- instrumentation ------------------------------------------------------
     def counters(self):

@@ -132,3 +132,29 @@ def test_server_warm_start_and_budget(cases):
         fo, _ = m.solve(rhs2, rel_tol=REL_TOL)
         l2, mx = _rel(_zm(fi), _zm(fo))
         assert l2 <= 1e-8 and mx <= 1e-8
+
+
+def test_autotune_then_batch(cases):
+    """Tuned settings stay in their candidate sets, the tuned single-grid
+    solve still converges to the oracle's solution, and a batch of tuned
+    members (different sweep counts and smoother widths) matches them."""
+    sub = cases[:3]
+    members = [mg.Multigrid(*c[:3]) for c in sub]
+    tuned = [m.autotune(c[3]) for m, c in zip(members, sub)]
+    for t in tuned:
+        assert t["nu"] in (1, 2, 3) and t["inner_cycles"] in (2, 3, 4, 6)
+        assert set(t["line_threads"]) <= {128, 256} and t["candidates"] >= 13
+    with mg.Batch(members) as b:
+        fis, sts = b.solve([c[3] for c in sub], rel_tol=REL_TOL)
+    for m, c, fi, st in zip(members, sub, fis, sts):
+        assert st["status"] == mg.OK and st["rel_residual"] <= REL_TOL
+        fo, so = m.solve(c[3], rel_tol=REL_TOL)
+        assert so["status"] == mg.OK
+        l2, mx = _rel(_zm(fi), _zm(fo))
+        assert l2 <= 1e-9 and mx <= 1e-9
+    x, y, z, r = sub[2]
+    ref, *_ = Oracle(x, y, z, islor=1).multi(r, eps=1e-13, ficycle=400)
+    l2, mx = _rel(_zm(fis[2]), _zm(ref))
+    assert l2 <= 1e-8 and mx <= 1e-8
+    for m in members:
+        m.close()
