@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define PLES_MG_ABI_VERSION 1
+#define PLES_MG_ABI_VERSION 2
 
 /* status codes */
 enum {
@@ -66,6 +66,12 @@ typedef struct {
                               2 = zebra with its rows staged by TMA (FP32) */
     int coarsening;        /* 0 = full, the reference's hierarchy (mul_met);
                               1 = semi-coarsening where x/z spacings differ     */
+    const unsigned char *solid; /* immersed-boundary mask (1:jx,1:jy,1:jz), 1 =
+                              solid cell, or NULL.  No counterpart in the
+                              reference's multigrid: solid cells are removed
+                              from the system (Neumann at their faces); the
+                              solution is 0 there and rhs, compatibility and
+                              mean refer to the fluid cells.  Not for batches. */
 } ples_mg_desc;
 
 typedef struct {

@@ -128,8 +128,8 @@ __global__ void kb_add(WALK_ARGS) {
     walk(t, n, total, ctr, st, ph, [st](const AddTask& k, const Blk& B) {
         const InstState& S = st[k.h.inst];
         const double v = -(k.use_mean ? S.mean : S.shift);
-        if (k.box) k_add_box_blk(k.g, k.a, v, B);
-        else k_add_interior_blk(k.g, k.a, v, B);
+        if (k.box) k_add_box_blk(k.g, k.a, v, nullptr, B);
+        else k_add_interior_blk(k.g, k.a, v, nullptr, B);
     });
 }
 template <class T>
@@ -647,6 +647,7 @@ int batch_create(ples_mg_handle* const* members, int n, ples_mg_batch* b) {
             return bfail(b, PLES_MG_BAD_ARG,
                          "member %d: batched solves need mixed precision, the zebra smoother and full coarsening", i);
         if (!h->coarse_S) return bfail(b, PLES_MG_BAD_ARG, "member %d: coarsest level too large for the dense solve", i);
+        if (h->masked) return bfail(b, PLES_MG_BAD_ARG, "member %d: immersed-boundary masks are not batched", i);
         if (h->nu_pre != h->nu_post)
             return bfail(b, PLES_MG_BAD_ARG, "member %d: batched solves need nu_pre == nu_post", i);
         for (int l = 1; l < h->nlev; ++l)

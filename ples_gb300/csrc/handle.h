@@ -56,6 +56,10 @@ struct ples_mg_handle {
     double* cs_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // their device buffers
     void* coarse_S = nullptr;                            // dense inverse of the coarsest system (T)
     int coarse_n = 0;
+    // immersed-boundary mask: byte box per level (1 = solid), fluid cells of level 1
+    bool masked = false;
+    uint8_t* mask[kMaxLev] = {};
+    long long nfluid = 0;
     int wall_passes = 3;
     double wall_q = 0.0;
     int nu_pre = 2, nu_post = 2, nu_coarse = 40, inner_cycles = 3, smoother = 0;

@@ -161,12 +161,14 @@ __global__ void __launch_bounds__(256) k_line_relax_tma(const __grid_constant__ 
                 if (!odd && !noneigh) f += Y2[yj] * (P0(1, 1) + P0(1, 0) - P0(-1, 1) - P0(-1, 0));
                 a = 0.f;
                 im = 1.f / Y1[yj];
+                if (Y1[yj] == 0.f) { im = 1.f; f = 0.f; }  // wall row above a solid cell
             } else if (j == ny + 1) {
                 const float a2 = Y1[yjm];  // face ny
                 f = noneigh ? 0.f : -(Y3[yjm] * (PP(0, 0) + PP(0, -1) - PM(0, 0) - PM(0, -1)));
                 if (!odd && !noneigh) f -= Y2[yjm] * (P0(1, 0) + P0(1, -1) - P0(-1, 0) - P0(-1, -1));
                 a = -a2;
                 im = 1.f / (a2 - a * cpm);
+                if (a2 == 0.f) { im = 1.f; f = 0.f; }  // wall row below a solid cell
             } else {
                 const float a1e = X1[cx], a1w = X1[cx - 1];
                 const float a3f = Z1[zf], a3b = Z1[zb];
@@ -175,6 +177,11 @@ __global__ void __launch_bounds__(256) k_line_relax_tma(const __grid_constant__ 
                 const float bd = -(a2 + a + a1e + a1w + a3f + a3b);
                 im = 1.f / (bd - a * cpm);
                 f = b[ChunkLayout::RH + jj * 32 + lane];
+                if (bd == 0.f) {  // solid cell of an immersed-boundary mask: identity row
+                    im = 1.f;
+                    f = 0.f;
+                    a = 0.f;
+                }
                 if (!noneigh) {
                     const float pn = P0(0, 1), ps = P0(0, -1);
                     const float pf = PP(0, 0), pb = PM(0, 0);

@@ -170,6 +170,58 @@ __global__ void k_ghost_xz(Geom g, T* __restrict__ p) {
 }
 
 // ---------------------------------------------------------------------------
+// Immersed-boundary mask (no counterpart in the reference's multigrid).  m is
+// a byte box of the level: 1 = solid cell; the periodic ghost shell holds the
+// images and each wall ghost row the value of the interior cell next to it.
+// A face that touches a solid cell carries no flux (Neumann at the immersed
+// boundary): its normal and cross coefficients are zeroed.  A cross
+// coefficient of a fluid-fluid face is zeroed too when its tangential stencil
+// reaches a solid cell, so the operator of the fluid cells reads fluid values
+// only and keeps constants in its null space.  A solid cell is left with all
+// coefficients zero: the smoothers treat such rows as identity rows.
+template <typename T>
+__global__ void k_mask_coef(Geom g, Coef<T> c, const uint8_t* __restrict__ m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long q = g.at(i, j, k), sj = g.sj, sk = g.sk;
+    auto S = [&](long long r) { return m[r] != 0; };
+    if (j >= 1) {  // csi face i+1/2 of cell (i,j,k)
+        if (S(q) || S(q + 1)) {
+            c.a1[q] = T(0); c.b12[q] = T(0); c.b13[q] = T(0);
+        } else {
+            if (S(q + sj) || S(q - sj) || S(q + 1 + sj) || S(q + 1 - sj)) c.b12[q] = T(0);
+            if (k >= 1 && (S(q + sk) || S(q - sk) || S(q + 1 + sk) || S(q + 1 - sk))) c.b13[q] = T(0);
+        }
+    }
+    if (i >= 1 && k >= 1) {  // eta face j+1/2
+        if (S(q) || S(q + sj)) {
+            c.a2[q] = T(0); c.b21[q] = T(0); c.b23[q] = T(0);
+        } else {
+            if (S(q + 1) || S(q - 1) || S(q + 1 + sj) || S(q - 1 + sj)) c.b21[q] = T(0);
+            if (S(q + sk) || S(q - sk) || S(q + sj + sk) || S(q + sj - sk)) c.b23[q] = T(0);
+        }
+    }
+    if (i >= 1 && j >= 1) {  // zeta face k+1/2
+        if (S(q) || S(q + sk)) {
+            c.a3[q] = T(0); c.b31[q] = T(0); c.b32[q] = T(0);
+        } else {
+            if (S(q + 1) || S(q - 1) || S(q + 1 + sk) || S(q - 1 + sk)) c.b31[q] = T(0);
+            if (S(q + sj) || S(q - sj) || S(q + sj + sk) || S(q - sj + sk)) c.b32[q] = T(0);
+        }
+    }
+}
+
+// zero a field on the solid cells of the mask (the whole box)
+template <typename T>
+__global__ void k_zero_solid(Geom g, T* __restrict__ p, const uint8_t* __restrict__ m) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.n;
+         q += (long long)gridDim.x * blockDim.x)
+        if (m[q]) p[q] = T(0);
+}
+
+// ---------------------------------------------------------------------------
 // The two first-order recurrences of a Thomas solve with a precomputed LU
 // factor, for the 32 lines (lanes) held in shared memory [nj][32]:
 //   forward  d(j) = G(j) - AL(j) d(j-1),  d(0) = G(0)
@@ -239,13 +291,15 @@ __global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int k = blockIdx.y + 1;
     if (i > g.nx) return;
-    T prev = T(-1);
+    // a row whose coefficients are all zero (a solid cell of an immersed-
+    // boundary mask, or the wall row next to one) is an identity row: c' = 0
+    T prev = ld(c.a2, g.at(i, 0, k)) == T(0) ? T(0) : T(-1);
     cp[g.at(i, 0, k)] = prev;
     for (int j = 1; j <= g.ny; ++j) {
         const long long q = g.at(i, j, k);
         const T a = ld(c.a2, q - g.sj), cc = ld(c.a2, q);
         const T b = -(cc + a + ld(c.a1, q) + ld(c.a1, q - 1) + ld(c.a3, q) + ld(c.a3, q - g.sk));
-        prev = cc / (b - a * prev);
+        prev = b == T(0) ? T(0) : cc / (b - a * prev);
         cp[q] = prev;
     }
     cp[g.at(i, g.ny + 1, k)] = T(0);
@@ -410,6 +464,7 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
                     f += ld(c.b21, q) * (P(j, 1, 1, 0) + P(j, 1, 0, 0) - P(j, -1, 1, 0) - P(j, -1, 0, 0));
                 a = T(0);
                 im = T(1) / a2;
+                if (a2 == T(0)) { im = T(1); f = T(0); }  // wall row above a solid cell
             } else if (j == ny + 1) {
                 const long long qn = q - sj;
                 const T a2 = ld(c.a2, qn);
@@ -419,6 +474,7 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
                     f -= ld(c.b21, qn) * (P(j, 1, 0, 0) + P(j, 1, -1, 0) - P(j, -1, 0, 0) - P(j, -1, -1, 0));
                 a = -a2;
                 im = T(1) / (a2 - a * ld(cpa, qn));
+                if (a2 == T(0)) { im = T(1); f = T(0); }  // wall row below a solid cell
             } else {
                 const T a1e = ld(c.a1, q), a1w = ld(c.a1, q - 1);
                 const T a3f = ld(c.a3, q), a3b = ld(c.a3, q - sk);
@@ -427,6 +483,11 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
                 const T b = -(a2 + a + a1e + a1w + a3f + a3b);
                 im = T(1) / (b - a * ld(cpa, q - sj));
                 f = ld(rh, q);
+                if (b == T(0)) {  // solid cell of an immersed-boundary mask: identity row
+                    im = T(1);
+                    f = T(0);
+                    a = T(0);
+                }
                 if (!noneigh) {
                     const T pn = P(j, 0, 1, 0), ps = P(j, 0, -1, 0);
                     const T pf = P(j, 0, 0, 1), pb = P(j, 0, 0, -1);

@@ -109,17 +109,25 @@ __device__ __forceinline__ void k_sum_interior_blk(Geom g, const double* __restr
     if (threadIdx.x == 0)
         psum[((long long)B.z * B.gy + B.y) * B.gx + B.x] = s;
 }
-__device__ __forceinline__ void k_add_interior_blk(Geom g, double* __restrict__ a, double v, const Blk& B) {
+__device__ __forceinline__ void k_add_interior_blk(Geom g, double* __restrict__ a, double v,
+                                                   const uint8_t* __restrict__ solid, const Blk& B) {
     const int i = B.x * blockDim.x + threadIdx.x + 1;
     const int j = B.y * blockDim.y + threadIdx.y + 1;
     const int k = B.z + 1;
-    if (i <= g.nx && j <= g.ny) a[g.at(i, j, k)] += v;
+    if (i <= g.nx && j <= g.ny) {
+        const long long q = g.at(i, j, k);
+        if (!solid || !solid[q]) a[q] += v;
+    }
 }
-__device__ __forceinline__ void k_add_box_blk(Geom g, double* __restrict__ a, double v, const Blk& B) {
+__device__ __forceinline__ void k_add_box_blk(Geom g, double* __restrict__ a, double v,
+                                              const uint8_t* __restrict__ solid, const Blk& B) {
     const int i = B.x * blockDim.x + threadIdx.x;
     const int j = B.y * blockDim.y + threadIdx.y;
     const int k = B.z;
-    if (i <= g.nx + 1 && j <= g.ny + 1) a[g.at(i, j, k)] += v;
+    if (i <= g.nx + 1 && j <= g.ny + 1) {
+        const long long q = g.at(i, j, k);
+        if (!solid || !solid[q]) a[q] += v;
+    }
 }
 template <typename Te>
 __device__ __forceinline__ void k_update_blk(Geom g, double* __restrict__ x, const Te* __restrict__ e, const Blk& B) {
@@ -145,6 +153,10 @@ __device__ __forceinline__ void k_wall_compute_blk(Geom g, Coef<double> c, const
     if (side == 0) {
         const long long q0 = g.at(i, 0, k), q1 = q0 + sj;
         const double a2 = c.a2[q0];
+        if (a2 == 0.0) {  // above a solid cell of an immersed-boundary mask
+            w[widx] = 0.0;
+            return;
+        }
         double v = p[q1];
         if (cs3) v -= an_dt * cs3[(long long)(k - 1) * g.nx + (i - 1)] / a2;
         v += (c.b21[q0] * (p[q1 + 1] + p[q0 + 1] - p[q1 - 1] - p[q0 - 1]) +
@@ -153,6 +165,10 @@ __device__ __forceinline__ void k_wall_compute_blk(Geom g, Coef<double> c, const
     } else {
         const long long qt = g.at(i, g.ny + 1, k), qn = qt - sj;
         const double a2 = c.a2[qn];
+        if (a2 == 0.0) {
+            w[widx] = 0.0;
+            return;
+        }
         double v = p[qn];
         if (cs4) v += an_dt * cs4[(long long)(k - 1) * g.nx + (i - 1)] / a2;
         v -= (c.b21[qn] * (p[qt + 1] + p[qn + 1] - p[qt - 1] - p[qn - 1]) +

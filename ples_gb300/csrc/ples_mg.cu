@@ -75,12 +75,12 @@ __global__ void k_reduce_final(const double* __restrict__ a, const double* __res
     if (threadIdx.x == 0) { out[0] = s; out[1] = m; }
 }
 
-__global__ void k_add_interior(Geom g, double* __restrict__ a, double v) {
-    k_add_interior_blk(g, a, v, hw_blk());
+__global__ void k_add_interior(Geom g, double* __restrict__ a, double v, const uint8_t* __restrict__ solid) {
+    k_add_interior_blk(g, a, v, solid, hw_blk());
 }
 
-__global__ void k_add_box(Geom g, double* __restrict__ a, double v) {
-    k_add_box_blk(g, a, v, hw_blk());
+__global__ void k_add_box(Geom g, double* __restrict__ a, double v, const uint8_t* __restrict__ solid) {
+    k_add_box_blk(g, a, v, solid, hw_blk());
 }
 
 template <typename Te>
@@ -103,8 +103,10 @@ __global__ void k_wall_contraction(Geom g, Coef<double> c, unsigned long long* o
     const int k = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > g.nx || k > g.nz) return;
     const long long q0 = g.at(i, 0, k), qn = g.at(i, g.ny, k);
-    double v = fmax(2.0 * (fabs(c.b21[q0]) + fabs(c.b23[q0])) / c.a2[q0],
-                    2.0 * (fabs(c.b21[qn]) + fabs(c.b23[qn])) / c.a2[qn]);
+    // wall rows next to solid cells (a2 = 0) are fixed at zero: no contraction
+    const double v0 = c.a2[q0] != 0.0 ? 2.0 * (fabs(c.b21[q0]) + fabs(c.b23[q0])) / c.a2[q0] : 0.0;
+    const double vn = c.a2[qn] != 0.0 ? 2.0 * (fabs(c.b21[qn]) + fabs(c.b23[qn])) / c.a2[qn] : 0.0;
+    const double v = fmax(v0, vn);
     atomicMax(out, (unsigned long long)__double_as_longlong(v));
 }
 
@@ -489,7 +491,13 @@ template <typename T>
 int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles, ples_mg_stats* st) {
     LevelData& F = h->L[0];
     const Geom& g = F.g;
-    const double N = (double)g.nx * g.ny * g.nz;
+    // cells in the system: all interior cells, or the fluid ones of a mask
+    const double N = h->masked ? (double)h->nfluid : (double)g.nx * g.ny * g.nz;
+    if (h->masked) {  // the solution and rhs vanish on solid cells
+        k_zero_solid<double><<<grid1(g.n), 256, 0, h->st>>>(g, h->x, h->mask[0]);
+        k_zero_solid<double><<<grid1(g.n), 256, 0, h->st>>>(g, h->b, h->mask[0]);
+        h->launches += 2;
+    }
     const double dt = h->d.dt;
     // the caller's ghost layer is arbitrary: make the periodic shell consistent
     ghost_xz<double>(h, g, h->x);
@@ -515,7 +523,7 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     const double shift = (sb - flux) / N;
     {
         dim3 blk(32, 4), grd((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
-        k_add_interior<<<grd, blk, 0, h->st>>>(g, h->b, -shift);
+        k_add_interior<<<grd, blk, 0, h->st>>>(g, h->b, -shift, h->mask[0]);
         ++h->launches;
     }
     double bn2 = 0.0;
@@ -561,11 +569,16 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         CK(cudaGetLastError());
         ++it;
     }
-    // zero-mean solution (Neumann null space)
+    // zero-mean solution (Neumann null space).  Solid cells of a mask are
+    // decoupled unknowns that the prolongation may have touched: reset them.
+    if (h->masked) {
+        k_zero_solid<double><<<grid1(g.n), 256, 0, h->st>>>(g, h->x, h->mask[0]);
+        ++h->launches;
+    }
     double sx = 0.0;
     rc = sum_interior(h, h->x, 0, &sx);
     if (rc) return rc;
-    k_add_box<<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, -sx / N);
+    k_add_box<<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, -sx / N, h->mask[0]);
     ++h->launches;
     CK(cudaGetLastError());
     st->outer_iterations = it;
@@ -694,7 +707,20 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
                     R[n] = 1.0;
                 }
             }
-    for (int u = 0; u < n; ++u) K[(size_t)n * m + u] = 1.0;
+    // rows without any coefficient (solid cells of a mask and the wall rows
+    // next to them) become identity rows outside the null space and the mean
+    for (int u = 0; u < n; ++u) {
+        double* R = &K[(size_t)u * m];
+        double sum = 0.0;
+        for (int v = 0; v < n; ++v) sum += std::fabs(R[v]);
+        if (sum == 0.0) {
+            R[u] = 1.0;
+            R[n] = 0.0;
+            K[(size_t)n * m + u] = 0.0;
+        } else {
+            K[(size_t)n * m + u] = 1.0;
+        }
+    }
     // Gauss-Jordan inverse with partial pivoting
     std::vector<double> I((size_t)m * m, 0.0);
     for (int u = 0; u < m; ++u) I[(size_t)u * m + u] = 1.0;
@@ -732,6 +758,65 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
     CK(cudaStreamSynchronize(h->st));
     h->coarse_n = n;
     return PLES_MG_OK;
+}
+
+// Immersed-boundary masks of every level as byte boxes (1 = solid) with
+// their ghost cells: periodic images in x and z, and each wall ghost row a
+// copy of the interior row next to it.  A coarse cell is solid when all its
+// children are.  solid: (1:jx,1:jy,1:jz) of the fine grid.
+int build_masks(ples_mg_handle* h, const unsigned char* solid) {
+    std::vector<uint8_t> prev;  // interior mask of the finer level, (nx,ny,nz)
+    for (int n = 0; n < h->nlev; ++n) {
+        const Geom& g = h->L[n].g;
+        std::vector<uint8_t> in((size_t)g.nx * g.ny * g.nz);
+        auto I = [&](const Geom& gg, int i, int j, int k) { return ((size_t)(k - 1) * gg.ny + (j - 1)) * gg.nx + (i - 1); };
+        if (n == 0) {
+            long long nf = 0;
+            for (size_t q = 0; q < in.size(); ++q) {
+                in[q] = solid[q] ? 1 : 0;
+                nf += in[q] ? 0 : 1;
+            }
+            h->nfluid = nf;
+            if (nf == 0) return fail(h, PLES_MG_BAD_ARG, "the immersed-boundary mask leaves no fluid cell");
+        } else {
+            const Geom& gf = h->L[n - 1].g;
+            const LevelData& C = h->L[n];
+            for (int k = 1; k <= g.nz; ++k)
+                for (int j = 1; j <= g.ny; ++j)
+                    for (int i = 1; i <= g.nx; ++i) {
+                        bool all = true;
+                        for (int dk = 0; dk < C.rz; ++dk)
+                            for (int dj = 0; dj < C.ry; ++dj)
+                                for (int di = 0; di < C.rx; ++di)
+                                    all = all && prev[I(gf, C.rx * i - di, C.ry * j - dj, C.rz * k - dk)];
+                        in[I(g, i, j, k)] = all ? 1 : 0;
+                    }
+        }
+        std::vector<uint8_t> box((size_t)g.n, 0);
+        for (int k = 0; k <= g.nz + 1; ++k)
+            for (int j = 0; j <= g.ny + 1; ++j)
+                for (int i = 0; i <= g.nx + 1; ++i) {
+                    const int si = i == 0 ? g.nx : (i == g.nx + 1 ? 1 : i);
+                    const int sk = k == 0 ? g.nz : (k == g.nz + 1 ? 1 : k);
+                    const int sj = j == 0 ? 1 : (j == g.ny + 1 ? g.ny : j);
+                    box[(size_t)g.at(i, j, k)] = in[I(g, si, sj, sk)];
+                }
+        int rc = dalloc(h, (void**)&h->mask[n], (size_t)g.n);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(h->mask[n], box.data(), (size_t)g.n, cudaMemcpyHostToDevice, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        prev.swap(in);
+    }
+    h->masked = true;
+    return PLES_MG_OK;
+}
+
+template <typename T>
+void mask_coef(ples_mg_handle* h, int lev, Coef<T>& c) {
+    const Geom& g = h->L[lev - 1].g;
+    k_mask_coef<T><<<dim3((g.nx + 1 + 31) / 32, (g.ny + 1 + 3) / 4, g.nz + 1), dim3(32, 4), 0, h->st>>>(
+        g, c, h->mask[lev - 1]);
+    ++h->launches;
 }
 
 constexpr int kDenseMax = 640;  // largest coarsest system solved by the dense inverse
@@ -812,6 +897,7 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
             L.post = 1.0;
         }
     }
+    if (d->solid && (rc = build_masks(h, d->solid))) return rc;
     if ((rc = dalloc(h, (void**)&h->xn, nn * 8)) || (rc = dalloc(h, (void**)&h->yn, nn * 8)) ||
         (rc = dalloc(h, (void**)&h->zn, nn * 8)))
         return rc;
@@ -828,10 +914,12 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         if ((rc = raw_metric(h, n, gr, tmp))) return rc;
         if (n == 1 || !mixed) {
             if ((rc = alloc_coef(h, L.g, L.cd)) || (rc = scale_into(h, n, gr, L.cd))) { free_tmp(tmp); return rc; }
+            if (h->masked) mask_coef(h, n, L.cd);
             L.has_cd = true;
         }
         if (mixed) {
             if ((rc = alloc_coef(h, L.g, L.cf)) || (rc = scale_into(h, n, gr, L.cf))) { free_tmp(tmp); return rc; }
+            if (h->masked) mask_coef(h, n, L.cf);
             L.has_cf = true;
         }
         CK(cudaStreamSynchronize(h->st));

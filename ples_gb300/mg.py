@@ -40,7 +40,8 @@ class Desc(C.Structure):
                 ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
                 ("z", C.POINTER(C.c_double)), ("dt", C.c_double), ("device", C.c_int),
                 ("nu_pre", C.c_int), ("nu_post", C.c_int), ("nu_coarse", C.c_int),
-                ("inner_cycles", C.c_int), ("smoother", C.c_int), ("coarsening", C.c_int)]
+                ("inner_cycles", C.c_int), ("smoother", C.c_int), ("coarsening", C.c_int),
+                ("solid", C.c_void_p)]
 
 
 class Tuning(C.Structure):
@@ -141,7 +142,7 @@ class Multigrid:
 
     def __init__(self, x, y, z, ip=0, jp=1, kp=0, precision="mixed", dt=1.0, device=0,
                  nlevmax=0, omega=0.0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0,
-                 smoother=0, coarsening=0, coords_layout=COORDS_NODES):
+                 smoother=0, coarsening=0, coords_layout=COORDS_NODES, solid=None):
         self._L = load()
         self._x, self._y, self._z = _f64(x), _f64(y), _f64(z)
         if coords_layout == COORDS_NODES:
@@ -160,6 +161,12 @@ class Multigrid:
         d.dt, d.device = dt, device
         d.nu_pre, d.nu_post, d.nu_coarse = nu_pre, nu_post, nu_coarse
         d.inner_cycles, d.smoother, d.coarsening = inner_cycles, smoother, coarsening
+        self._solid = None
+        if solid is not None:  # immersed-boundary mask (jx, jy, jz), nonzero = solid
+            self._solid = np.asfortranarray(np.asarray(solid) != 0, dtype=np.uint8)
+            if self._solid.shape != (jx, jy, jz):
+                raise ValueError(f"solid mask must be {(jx, jy, jz)}")
+            d.solid = self._solid.ctypes.data
         h = C.c_void_p()
         rc = self._L.ples_mg_create(C.byref(d), C.byref(h))
         if rc != OK:

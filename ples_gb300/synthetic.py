@@ -39,6 +39,7 @@ __all__ = [
     "serve_members",
     "poisson_arrivals",
     "next_rhs",
+    "sphere_mask",
 ]
 
 
@@ -184,3 +185,28 @@ def next_rhs(rhs, rng, frac=0.05):
     """The next time step's right-hand side of a member."""
     r = rhs + frac * rng.standard_normal(rhs.shape)
     return np.asfortranarray(r - r.mean())
+
+
+def sphere_mask(x, y, z, n=32, rmin=0.05, rmax=0.2, seed=11, lx=2.0 * math.pi, lz=math.pi):
+    """Immersed-boundary mask (jx, jy, jz), True = solid: n spheres with
+    centres uniform in the box [0,lx] x [min y, max y] x [0,lz] and radius
+    U(rmin, rmax), drawn with default_rng(seed) in the order (cx, cy, cz, r)
+    per sphere; a cell is solid when its centroid (mean of its 8 nodes) lies
+    inside a sphere, distances periodic in x and z."""
+    rng = np.random.default_rng(seed)
+    cx = 0.125 * sum(x[a:a + x.shape[0] - 1, b:b + x.shape[1] - 1, c:c + x.shape[2] - 1]
+                     for a in (0, 1) for b in (0, 1) for c in (0, 1))
+    cy = 0.125 * sum(y[a:a + y.shape[0] - 1, b:b + y.shape[1] - 1, c:c + y.shape[2] - 1]
+                     for a in (0, 1) for b in (0, 1) for c in (0, 1))
+    cz = 0.125 * sum(z[a:a + z.shape[0] - 1, b:b + z.shape[1] - 1, c:c + z.shape[2] - 1]
+                     for a in (0, 1) for b in (0, 1) for c in (0, 1))
+    y0, y1 = float(y.min()), float(y.max())
+    solid = np.zeros(cx.shape, dtype=bool)
+    for _ in range(n):
+        sx, sy, sz, r = rng.uniform(0, lx), rng.uniform(y0, y1), rng.uniform(0, lz), rng.uniform(rmin, rmax)
+        dx = np.abs(cx - sx)
+        dx = np.minimum(dx, lx - dx)
+        dz = np.abs(cz - sz)
+        dz = np.minimum(dz, lz - dz)
+        solid |= dx * dx + (cy - sy) ** 2 + dz * dz < r * r
+    return np.asfortranarray(solid)
