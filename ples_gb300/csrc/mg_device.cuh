@@ -34,6 +34,12 @@ namespace ples {
 
 constexpr int kOX = 31;  // element offset of i = 0 inside a row
 
+// resident CTAs per SM the FP32 line smoother is compiled for (its register
+// budget: 65536 / (256 * this)); 4 measured fastest on GB300 (2-6 tried)
+#ifndef PLES_LINE_MIN_BLOCKS
+#define PLES_LINE_MIN_BLOCKS 4
+#endif
+
 struct Geom {
     int nx, ny, nz;
     int sj;          // row pitch (elements)
@@ -532,7 +538,7 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
     }
 }
 template <typename T, bool ZEBRA, bool ZIN>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? PLES_LINE_MIN_BLOCKS : 2) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
                                                     int kpar, int zk) {
