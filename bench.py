@@ -120,6 +120,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_throughput(t_local, steps, world_size, dist=None, device="cpu"):
+    """Whole-job throughput of independent replicas: every rank timed its own
+    `steps` solves in t_local seconds; the job's time is the slowest rank's
+    (max over ranks) and the job solved steps x world_size grids.  Returns
+    (t_max, solves per second)."""
+    t = t_local
+    if dist is not None and world_size > 1:
+        import torch
+        tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return t, steps * world_size / t
+
+
 def cpu_baseline(workload, threads_cap=None, cycles=1):
     """Reference algorithm on the host: the CPU oracle (line SOR as in the
     reference's islor=1 option, 4 levels, kss 5/10, omega 1.6) with nproc
@@ -274,11 +288,7 @@ def main():
     launches = m.counters()["launches"] - n0
     kms, kn = m.kernel_time()
     m.time_kernel(None)
-    if dist:
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-    value = args.steps * ws / t
+    t, value = replica_throughput(t, args.steps, ws, dist, device="cuda")
     ms_per_step = t / args.steps * 1e3
     outer = statistics.mean(s["outer_iterations"] for s in stats)
     relres = max(s["rel_residual"] for s in stats)

@@ -75,6 +75,17 @@ struct ples_mg_handle {
     size_t ev_used = 0;
     double timed_ms = 0.0;
     long long timed_launches = 0;
+    // CUDA graph of one outer iteration (V-cycles, update, wall fill, FP64
+    // residual, reduction and its copy to the host), replayed while the
+    // settings it was captured with hold
+    cudaGraphExec_t iter_exec = nullptr;
+    std::vector<long long> iter_key;
+    long long iter_launches = 0;
+    bool use_graphs = true;
+    bool capturing = false;            // timing events go into the graph
+    std::vector<cudaEvent_t> ev_graph; // the graph's timing event pairs
+    size_t g_used = 0;
+    bool graph_pending = false;        // a replay ran since the last collect
 };
 
 inline int fail(ples_mg_handle* h, int code, const char* fmt, ...) {

@@ -149,32 +149,49 @@ namespace {
 // kernel kinds for the optional event timing
 enum { KIND_LINE = 0, KIND_RESTRICT = 1, KIND_PROLONG = 2, KIND_OUTER = 3, KIND_COARSE = 4, KIND_WALL = 5 };
 
+// Event pairs around the timed kernel kind.  Outside a graph capture they
+// come from ev_pool and are read once; while the outer-iteration graph is
+// captured they come from ev_graph and are recorded as event nodes of the
+// graph, read after every replay.
 void timed_begin(ples_mg_handle* h, int kind, int level) {
     if (h->timed_kind != kind || h->timed_level != level) return;
-    if (h->ev_used + 2 > h->ev_pool.size()) {
+    std::vector<cudaEvent_t>& pool = h->capturing ? h->ev_graph : h->ev_pool;
+    size_t& used = h->capturing ? h->g_used : h->ev_used;
+    if (used + 2 > pool.size()) {
         for (int q = 0; q < 64; ++q) {
             cudaEvent_t e;
             cudaEventCreate(&e);
-            h->ev_pool.push_back(e);
+            pool.push_back(e);
         }
     }
-    cudaEventRecord(h->ev_pool[h->ev_used], h->st);
+    if (h->capturing) cudaEventRecordWithFlags(pool[used], h->st, cudaEventRecordExternal);
+    else cudaEventRecord(pool[used], h->st);
 }
 void timed_end(ples_mg_handle* h, int kind, int level) {
     if (h->timed_kind != kind || h->timed_level != level) return;
-    cudaEventRecord(h->ev_pool[h->ev_used + 1], h->st);
-    h->ev_used += 2;
+    if (h->capturing) {
+        cudaEventRecordWithFlags(h->ev_graph[h->g_used + 1], h->st, cudaEventRecordExternal);
+        h->g_used += 2;
+    } else {
+        cudaEventRecord(h->ev_pool[h->ev_used + 1], h->st);
+        h->ev_used += 2;
+    }
 }
 // after a stream synchronisation: fold recorded pairs into the totals
 void timed_collect(ples_mg_handle* h) {
-    for (size_t q = 0; q + 1 < h->ev_used; q += 2) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, h->ev_pool[q], h->ev_pool[q + 1]) == cudaSuccess) {
-            h->timed_ms += ms;
-            h->timed_launches += 1;
+    auto fold = [&](const std::vector<cudaEvent_t>& pool, size_t used) {
+        for (size_t q = 0; q + 1 < used; q += 2) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, pool[q], pool[q + 1]) == cudaSuccess) {
+                h->timed_ms += ms;
+                h->timed_launches += 1;
+            }
         }
-    }
+    };
+    fold(h->ev_pool, h->ev_used);
     h->ev_used = 0;
+    if (h->graph_pending) fold(h->ev_graph, h->g_used);
+    h->graph_pending = false;
 }
 
 int dalloc(ples_mg_handle* h, void** p, size_t bytes) {
@@ -536,18 +553,78 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     constexpr int kKC = 8;
     const dim3 rg((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kKC - 1) / kKC);
     const long long nblk = (long long)rg.x * rg.y * rg.z;
-    double rel = 0.0, rmax = 0.0, rel0 = -1.0;
-    int it = 0, status = PLES_MG_NOT_CONVERGED, vcyc = 0;
-    for (;;) {
+    // the device work between two stop tests: the FP64 residual of x (after
+    // its wall fill) with its norms copied to h_red, preceded from the second
+    // test on by the V-cycles and the update
+    auto enqueue_residual = [&]() {
         wall_fill(h, h->x, h->cs_c[2], h->cs_c[3], 1.0 / dt, h->wall_passes, g, F.cd);
         timed_begin(h, KIND_OUTER, 1);
         k_resid_outer2<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b);
         timed_end(h, KIND_OUTER, 1);
+        k_reduce_final<<<1, 1024, 0, h->st>>>(h->part_a, h->part_b, nblk, h->red);
+        h->launches += 2;
+        cudaMemcpyAsync(h->h_red, h->red, 5 * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    };
+    auto enqueue_iteration = [&]() {
+        for (int c = 0; c < h->inner_cycles; ++c) vcycle<T>(h, c == 0);
+        k_update<T><<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, (const T*)F.p);
         ++h->launches;
-        CK(cudaGetLastError());
-        double r2[2];
-        rc = reduce_to_host(h, h->part_a, h->part_b, nblk, r2);
-        if (rc) return rc;
+        enqueue_residual();
+    };
+    // graph replays of enqueue_iteration (the timing events, if any, are
+    // nodes of the graph)
+    const bool graphs = h->use_graphs;
+    if (graphs) {
+        std::vector<long long> key = {(long long)sizeof(T), h->inner_cycles, h->nu_pre, h->nu_post, h->nu_coarse,
+                                      h->timed_kind, h->timed_level,
+                                      h->smoother, h->wall_passes, (long long)(uintptr_t)h->cs_c[2],
+                                      (long long)(uintptr_t)h->cs_c[3]};
+        double an = 1.0 / dt;
+        long long anb;
+        std::memcpy(&anb, &an, sizeof anb);
+        key.push_back(anb);
+        for (int n = 0; n < h->nlev; ++n) {
+            key.push_back(h->L[n].line_threads);
+            key.push_back((long long)(uintptr_t)h->L[n].p);
+        }
+        if (!h->iter_exec || key != h->iter_key) {
+            if (h->iter_exec) cudaGraphExecDestroy(h->iter_exec);
+            h->iter_exec = nullptr;
+            const long long l0 = h->launches;
+            void* p0 = h->L[0].p;
+            cudaGraph_t gr = nullptr;
+            CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+            h->capturing = true;
+            h->g_used = 0;
+            enqueue_iteration();
+            h->capturing = false;
+            const cudaError_t ce = cudaStreamEndCapture(h->st, &gr);
+            h->iter_launches = h->launches - l0;
+            h->launches = l0;
+            if (ce != cudaSuccess || !gr) return fail(h, PLES_MG_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ce));
+            const cudaError_t ie = cudaGraphInstantiate(&h->iter_exec, gr, 0);
+            cudaGraphDestroy(gr);
+            if (ie != cudaSuccess) return fail(h, PLES_MG_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(ie));
+            // the sweeps of one iteration swap each level's buffers an even
+            // number of times, so every replay starts from the same roles
+            if (h->L[0].p != p0) return fail(h, PLES_MG_BAD_ARG, "odd sweep count per outer iteration");
+            h->iter_key = key;
+        }
+    }
+    double rel = 0.0, rmax = 0.0, rel0 = -1.0;
+    int it = 0, status = PLES_MG_NOT_CONVERGED, vcyc = 0;
+    enqueue_residual();
+    CK(cudaGetLastError());
+    for (;;) {
+        CK(cudaStreamSynchronize(h->st));
+        timed_collect(h);
+        const double r2[2] = {h->h_red[0], h->h_red[1]};
+        int flag = 0;
+        std::memcpy(&flag, h->h_red + 4, sizeof flag);
+        if (flag) {
+            CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
+            return fail(h, PLES_MG_DEVICE_TIMEOUT, "a staged transfer of the line smoother did not complete");
+        }
         rel = std::sqrt(r2[0]) / bnorm;
         rmax = r2[1];
         if (!std::isfinite(rel)) { status = PLES_MG_DIVERGED; break; }
@@ -560,13 +637,15 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         if (it >= max_cycles) break;
         // inner solve of L e = r: V-cycles from e = 0 (F.rh holds r; the
         // residual kernel wrote it with a consistent ghost shell of zeros)
-        for (int c = 0; c < h->inner_cycles; ++c) {
-            vcycle<T>(h, c == 0);
-            ++vcyc;
+        if (graphs) {
+            CK(cudaGraphLaunch(h->iter_exec, h->st));
+            h->launches += h->iter_launches;
+            h->graph_pending = true;
+        } else {
+            enqueue_iteration();
         }
-        k_update<T><<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, (const T*)F.p);
-        ++h->launches;
         CK(cudaGetLastError());
+        vcyc += h->inner_cycles;
         ++it;
     }
     // zero-mean solution (Neumann null space).  Solid cells of a mask are
@@ -1112,6 +1191,8 @@ void ples_mg_destroy(ples_mg_handle* h) {
     if (h->st) cudaStreamSynchronize(h->st);
     for (void* p : h->allocs) cudaFree(p);
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+    if (h->iter_exec) cudaGraphExecDestroy(h->iter_exec);
+    for (cudaEvent_t e : h->ev_graph) cudaEventDestroy(e);
     if (h->h_red) cudaFreeHost(h->h_red);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
@@ -1375,6 +1456,7 @@ int ples_mg_kernel_timing(ples_mg_handle* h, int kind, int level) {
     h->timed_ms = 0.0;
     h->timed_launches = 0;
     h->ev_used = 0;
+    h->graph_pending = false;
     return PLES_MG_OK;
 }
 
