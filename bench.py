@@ -587,7 +587,8 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
     prof = os.path.join(ROOT, "profiles", f"line_relax_{args.workload}.json")
     if os.path.exists(prof):
         try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+            # per timed unit: one sweep = both k-parity launches
+            traffic = json.load(open(prof)).get("dram_bytes_per_sweep")
         except Exception:
             traffic = None
     cpu = None
