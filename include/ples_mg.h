@@ -156,6 +156,23 @@ int ples_mg_counters(ples_mg_handle *h, long long *launches, long long *device_b
 int ples_mg_kernel_timing(ples_mg_handle *h, int kind, int level);
 int ples_mg_kernel_time(ples_mg_handle *h, double *total_ms, long long *launches);
 
+/* ---- the projection step around the solve -------------------------------
+ * One call for the pressure-correction step of a PLES time step
+ * (fsrc/stratiParticle.f03:2845-2937, potenziale = 0, no free surface):
+ * diver (rhs = div(uc,vc,wc)/dt, fsrc/diver.f03:25-27), multi (the solve,
+ * warm-started from fi), gradie (fsrc/gradie.f03:30-116) and vel_up
+ * (fsrc/vel_up.f03:40-52, 188-285): uc -= dt cgra1 on i = 0..jx, vc -= dt
+ * cgra2 on j = 1..jy-1 (the wall faces keep their flux), wc -= dt cgra3 on
+ * k = 0..jz, and u,v,w += -dt/2 J^-1 grad(fi) at the cells with their
+ * periodic images.  Host arrays: uc (0:jx,1:jy,1:jz), vc (1:jx,0:jy,1:jz),
+ * wc (1:jx,1:jy,0:jz), u,v,w and fi (0:jx+1,0:jy+1,0:jz+1); u,v,w may all
+ * be NULL (contravariant part only).  dt is the descriptor's.  The face
+ * normals and the cell Jacobian are built on the device at the first call
+ * with u,v,w (nine face arrays and one cell array, FP64). */
+int ples_mg_project(ples_mg_handle *h, double *uc, double *vc, double *wc, double *u,
+                    double *v, double *w, double *fi, double rel_tol, int max_cycles,
+                    ples_mg_stats *stats);
+
 /* ---- autotuner ----------------------------------------------------------
  * No counterpart in the reference (its kss, nlevel and omega are fixed
  * inputs).  Times candidate settings on this handle's grid and keeps the

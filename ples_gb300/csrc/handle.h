@@ -54,6 +54,13 @@ struct ples_mg_handle {
     double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
     double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes
     double* cs_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // their device buffers
+    // projection step (diver / gradie / vel_up), allocated on first use:
+    // contravariant face velocities, Cartesian cell velocities, face normals
+    // csx..ztz and the cell Jacobian
+    double *d_uc = nullptr, *d_vc = nullptr, *d_wc = nullptr;
+    double *d_u = nullptr, *d_v = nullptr, *d_w = nullptr;
+    double* nrm[9] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double* giac = nullptr;
     void* coarse_S = nullptr;                            // dense inverse of the coarsest system (T)
     int coarse_n = 0;
     // immersed-boundary mask: byte box per level (1 = solid), fluid cells of level 1

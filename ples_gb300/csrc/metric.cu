@@ -94,7 +94,7 @@ __device__ void metric_row(int row, double xcsi, double ycsi, double zcsi, doubl
 
 // csi faces i = 0..nx (multigrid.f03:2520-2666 / metrica.f03:85-197)
 __global__ void k_metric_csi(Nodes N, Geom g, int sx, int sy, int sz, double inv_pot, double* g11, double* g12,
-                             double* g13) {
+                             double* g13, double* nx_, double* ny_, double* nz_) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
@@ -132,9 +132,15 @@ __global__ void k_metric_csi(Nodes N, Geom g, int sx, int sy, int sz, double inv
     const double xzet = .5 * (N.X(ic, j2, k2) + N.X(ic, j1, k2)) - .5 * (N.X(ic, j2, k1) + N.X(ic, j1, k1));
     const double yzet = .5 * (N.Y(ic, j2, k2) + N.Y(ic, j1, k2)) - .5 * (N.Y(ic, j2, k1) + N.Y(ic, j1, k1));
     const double zzet = .5 * (N.Z(ic, j2, k2) + N.Z(ic, j1, k2)) - .5 * (N.Z(ic, j2, k1) + N.Z(ic, j1, k1));
+    const long long q = g.at(i, j, k);
+    if (nx_) {  // J(-1) grad(csi) on the face: csx, csy, csz (metrica.f03:158-160)
+        nx_[q] = yeta * zzet - yzet * zeta;
+        ny_[q] = xzet * zeta - xeta * zzet;
+        nz_[q] = xeta * yzet - xzet * yeta;
+    }
+    if (!g11) return;
     double t[3];
     metric_row(0, xcsi, ycsi, zcsi, xeta, yeta, zeta, xzet, yzet, zzet, t);
-    const long long q = g.at(i, j, k);
     if (sx == 1 && sy == 1 && sz == 1) {
         g11[q] = t[0]; g12[q] = t[1]; g13[q] = t[2];
     } else {
@@ -144,7 +150,7 @@ __global__ void k_metric_csi(Nodes N, Geom g, int sx, int sy, int sz, double inv
 
 // eta faces j = 0..ny (multigrid.f03:2675-2827 / metrica.f03:203-294)
 __global__ void k_metric_eta(Nodes N, Geom g, int sx, int sy, int sz, double inv_pot, double* g21, double* g22,
-                             double* g23) {
+                             double* g23, double* nx_, double* ny_, double* nz_) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z + 1;
@@ -182,9 +188,15 @@ __global__ void k_metric_eta(Nodes N, Geom g, int sx, int sy, int sz, double inv
     const double zzet = .5 * (N.Z(i2, jc, k2) + N.Z(i1, jc, k2)) - .5 * (N.Z(i2, jc, k1) + N.Z(i1, jc, k1));
     const double xcsi = .5 * (N.X(i2, jc, k2) + N.X(i2, jc, k1)) - .5 * (N.X(i1, jc, k2) + N.X(i1, jc, k1));
     const double xzet = .5 * (N.X(i2, jc, k2) + N.X(i1, jc, k2)) - .5 * (N.X(i2, jc, k1) + N.X(i1, jc, k1));
+    const long long q = g.at(i, j, k);
+    if (nx_) {  // etx, ety, etz (metrica.f03:272-274)
+        nx_[q] = yzet * zcsi - ycsi * zzet;
+        ny_[q] = xcsi * zzet - xzet * zcsi;
+        nz_[q] = xzet * ycsi - xcsi * yzet;
+    }
+    if (!g21) return;
     double t[3];
     metric_row(1, xcsi, ycsi, zcsi, xeta, yeta, zeta, xzet, yzet, zzet, t);
-    const long long q = g.at(i, j, k);
     if (sx == 1 && sy == 1 && sz == 1) {
         g21[q] = t[0]; g22[q] = t[1]; g23[q] = t[2];
     } else {
@@ -194,7 +206,7 @@ __global__ void k_metric_eta(Nodes N, Geom g, int sx, int sy, int sz, double inv
 
 // zeta faces k = 0..nz (multigrid.f03:2836-2988 / metrica.f03:316-419)
 __global__ void k_metric_zet(Nodes N, Geom g, int sx, int sy, int sz, double inv_pot, double* g31, double* g32,
-                             double* g33) {
+                             double* g33, double* nx_, double* ny_, double* nz_) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z;
@@ -232,9 +244,15 @@ __global__ void k_metric_zet(Nodes N, Geom g, int sx, int sy, int sz, double inv
     const double zcsi = .5 * (N.Z(i2, j2, kc) + N.Z(i2, j1, kc)) - .5 * (N.Z(i1, j2, kc) + N.Z(i1, j1, kc));
     const double xcsi = .5 * (N.X(i2, j2, kc) + N.X(i2, j1, kc)) - .5 * (N.X(i1, j2, kc) + N.X(i1, j1, kc));
     const double xeta = .5 * (N.X(i2, j2, kc) + N.X(i1, j2, kc)) - .5 * (N.X(i2, j1, kc) + N.X(i1, j1, kc));
+    const long long q = g.at(i, j, k);
+    if (nx_) {  // ztx, zty, ztz (the zeta-face normals of metrica.f03)
+        nx_[q] = ycsi * zeta - yeta * zcsi;
+        ny_[q] = xeta * zcsi - xcsi * zeta;
+        nz_[q] = xcsi * yeta - xeta * ycsi;
+    }
+    if (!g31) return;
     double t[3];
     metric_row(2, xcsi, ycsi, zcsi, xeta, yeta, zeta, xzet, yzet, zzet, t);
-    const long long q = g.at(i, j, k);
     if (sx == 1 && sy == 1 && sz == 1) {
         g31[q] = t[0]; g32[q] = t[1]; g33[q] = t[2];
     } else {
@@ -247,12 +265,56 @@ cudaError_t launch_metric(const double* xn, const double* yn, const double* zn, 
                           double* const gout[9], cudaStream_t st) {
     Nodes N{xn, yn, zn, jx, jy, jz, ip, jp, kp};
     dim3 blk(32, 4);
-    k_metric_csi<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 3) / 4, g.nz), blk, 0, st>>>(N, g, sx, sy, sz, inv_div,
-                                                                                   gout[0], gout[1], gout[2]);
-    k_metric_eta<<<dim3((g.nx + 31) / 32, (g.ny + 1 + 3) / 4, g.nz), blk, 0, st>>>(N, g, sx, sy, sz, inv_div,
-                                                                                   gout[3], gout[4], gout[5]);
-    k_metric_zet<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz + 1), blk, 0, st>>>(N, g, sx, sy, sz, inv_div,
-                                                                                   gout[6], gout[7], gout[8]);
+    k_metric_csi<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 3) / 4, g.nz), blk, 0, st>>>(
+        N, g, sx, sy, sz, inv_div, gout[0], gout[1], gout[2], nullptr, nullptr, nullptr);
+    k_metric_eta<<<dim3((g.nx + 31) / 32, (g.ny + 1 + 3) / 4, g.nz), blk, 0, st>>>(
+        N, g, sx, sy, sz, inv_div, gout[3], gout[4], gout[5], nullptr, nullptr, nullptr);
+    k_metric_zet<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz + 1), blk, 0, st>>>(
+        N, g, sx, sy, sz, inv_div, gout[6], gout[7], gout[8], nullptr, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+// Cell Jacobian J of the fine grid at cell centres, from the averaged node
+// differences of the cell (metrica's giac; the oracle's build_giac).
+__global__ void k_giac(Nodes N, Geom g, double* __restrict__ giac) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+#define C4(F, a, b, c, d) (.25 * (N.F a + N.F b + N.F c + N.F d))
+    const double xcsi = C4(X, (i, j, k), (i, j, k - 1), (i, j - 1, k - 1), (i, j - 1, k)) -
+                        C4(X, (i - 1, j, k), (i - 1, j, k - 1), (i - 1, j - 1, k - 1), (i - 1, j - 1, k));
+    const double ycsi = C4(Y, (i, j, k), (i, j, k - 1), (i, j - 1, k - 1), (i, j - 1, k)) -
+                        C4(Y, (i - 1, j, k), (i - 1, j, k - 1), (i - 1, j - 1, k - 1), (i - 1, j - 1, k));
+    const double zcsi = C4(Z, (i, j, k), (i, j, k - 1), (i, j - 1, k - 1), (i, j - 1, k)) -
+                        C4(Z, (i - 1, j, k), (i - 1, j, k - 1), (i - 1, j - 1, k - 1), (i - 1, j - 1, k));
+    const double xeta = C4(X, (i, j, k), (i, j, k - 1), (i - 1, j, k - 1), (i - 1, j, k)) -
+                        C4(X, (i, j - 1, k), (i, j - 1, k - 1), (i - 1, j - 1, k - 1), (i - 1, j - 1, k));
+    const double yeta = C4(Y, (i, j, k), (i, j, k - 1), (i - 1, j, k - 1), (i - 1, j, k)) -
+                        C4(Y, (i, j - 1, k), (i, j - 1, k - 1), (i - 1, j - 1, k - 1), (i - 1, j - 1, k));
+    const double zeta = C4(Z, (i, j, k), (i, j, k - 1), (i - 1, j, k - 1), (i - 1, j, k)) -
+                        C4(Z, (i, j - 1, k), (i, j - 1, k - 1), (i - 1, j - 1, k - 1), (i - 1, j - 1, k));
+    const double xzet = C4(X, (i, j, k), (i, j - 1, k), (i - 1, j - 1, k), (i - 1, j, k)) -
+                        C4(X, (i, j, k - 1), (i, j - 1, k - 1), (i - 1, j - 1, k - 1), (i - 1, j, k - 1));
+    const double yzet = C4(Y, (i, j, k), (i, j - 1, k), (i - 1, j - 1, k), (i - 1, j, k)) -
+                        C4(Y, (i, j, k - 1), (i, j - 1, k - 1), (i - 1, j - 1, k - 1), (i - 1, j, k - 1));
+    const double zzet = C4(Z, (i, j, k), (i, j - 1, k), (i - 1, j - 1, k), (i - 1, j, k)) -
+                        C4(Z, (i, j, k - 1), (i, j - 1, k - 1), (i - 1, j - 1, k - 1), (i - 1, j, k - 1));
+#undef C4
+    giac[g.at(i, j, k)] = jac(xcsi, ycsi, zcsi, xeta, yeta, zeta, xzet, yzet, zzet);
+}
+
+cudaError_t launch_normals(const double* xn, const double* yn, const double* zn, int jx, int jy, int jz, int ip,
+                           int jp, int kp, Geom g, double* const nout[9], double* giac, cudaStream_t st) {
+    Nodes N{xn, yn, zn, jx, jy, jz, ip, jp, kp};
+    dim3 blk(32, 4);
+    k_metric_csi<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 3) / 4, g.nz), blk, 0, st>>>(
+        N, g, 1, 1, 1, 1.0, nullptr, nullptr, nullptr, nout[0], nout[1], nout[2]);
+    k_metric_eta<<<dim3((g.nx + 31) / 32, (g.ny + 1 + 3) / 4, g.nz), blk, 0, st>>>(
+        N, g, 1, 1, 1, 1.0, nullptr, nullptr, nullptr, nout[3], nout[4], nout[5]);
+    k_metric_zet<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz + 1), blk, 0, st>>>(
+        N, g, 1, 1, 1, 1.0, nullptr, nullptr, nullptr, nout[6], nout[7], nout[8]);
+    k_giac<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), blk, 0, st>>>(N, g, giac);
     return cudaGetLastError();
 }
 

@@ -13,4 +13,9 @@ namespace ples {
 cudaError_t launch_metric(const double* xn, const double* yn, const double* zn, int jx, int jy, int jz,
                           int ip, int jp, int kp, int sx, int sy, int sz, double inv_div, Geom g,
                           double* const gout[9], cudaStream_t st);
+// Fine-level face normals J grad(csi), J grad(eta), J grad(zeta) on their
+// faces (csx,csy,csz on csi faces; etx,ety,etz; ztx,zty,ztz) into nine boxes
+// of geometry g, and the cell Jacobian giac at the cells.
+cudaError_t launch_normals(const double* xn, const double* yn, const double* zn, int jx, int jy, int jz, int ip,
+                           int jp, int kp, Geom g, double* const nout[9], double* giac, cudaStream_t st);
 }  // namespace ples

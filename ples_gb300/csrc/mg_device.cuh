@@ -39,6 +39,10 @@ constexpr int kOX = 31;  // element offset of i = 0 inside a row
 #ifndef PLES_LINE_MIN_BLOCKS
 #define PLES_LINE_MIN_BLOCKS 4
 #endif
+// how many of its rows ahead a warp of the line smoother prefetches into L2
+#ifndef PLES_LINE_PF_ROWS
+#define PLES_LINE_PF_ROWS 1
+#endif
 
 struct Geom {
     int nx, ny, nz;
@@ -451,8 +455,21 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
     if (act) {
         for (int j = w; j < nj; j += nw) {
             const long long q = g.at(i, j, k);
-            if (j + nw < nj) {  // next row of this warp: start its lines towards L2
-                const long long qn = q + nw * sj;
+            // a later row of this warp (PLES_LINE_PF_ROWS rows ahead): start
+            // its lines towards L2; the first rows get theirs before the loop
+            if (j == w)
+                for (int d = 1; d < PLES_LINE_PF_ROWS && j + d * nw < nj; ++d) {
+                    const long long qn = q + d * nw * sj;
+                    pf_l2(c.a1, qn); pf_l2(c.b12, qn); pf_l2(c.b13, qn);
+                    pf_l2(c.a2, qn); pf_l2(c.b21, qn); pf_l2(c.b23, qn);
+                    pf_l2(c.a3, qn); pf_l2(c.b31, qn); pf_l2(c.b32, qn);
+                    pf_l2(c.a3, qn - sk); pf_l2(c.b31, qn - sk); pf_l2(c.b32, qn - sk);
+                    pf_l2(rh, qn); pf_l2(cpa, qn);
+                    if (!ZIN) pf_l2(pin, qn + sj);
+                    if (!zk) { pf_l2(pk, qn + sj + sk); pf_l2(pk, qn + sj - sk); }
+                }
+            if (j + PLES_LINE_PF_ROWS * nw < nj) {
+                const long long qn = q + PLES_LINE_PF_ROWS * nw * sj;
                 pf_l2(c.a1, qn); pf_l2(c.b12, qn); pf_l2(c.b13, qn);
                 pf_l2(c.a2, qn); pf_l2(c.b21, qn); pf_l2(c.b23, qn);
                 pf_l2(c.a3, qn); pf_l2(c.b31, qn); pf_l2(c.b32, qn);

@@ -1467,6 +1467,169 @@ int ples_mg_kernel_time(ples_mg_handle* h, double* total_ms, long long* launches
     return PLES_MG_OK;
 }
 
+// ---- projection step either side of the solve (the calls around multi at
+// fsrc/stratiParticle.f03:2845-2937: diver, multi, gradie, vel_up), for
+// potenziale = 0, no free surface, periodic x and z, walls in y
+
+}  // extern "C"
+
+namespace {
+
+// reference extents of the face velocities: uc(0:jx,1:jy,1:jz),
+// vc(1:jx,0:jy,1:jz), wc(1:jx,1:jy,0:jz); cell arrays (0:jx+1,0:jy+1,0:jz+1)
+__device__ __forceinline__ long long iuc(const Geom& g, int i, int j, int k) {
+    return ((long long)(k - 1) * g.ny + (j - 1)) * (g.nx + 1) + i;
+}
+__device__ __forceinline__ long long ivc(const Geom& g, int i, int j, int k) {
+    return ((long long)(k - 1) * (g.ny + 1) + j) * g.nx + (i - 1);
+}
+__device__ __forceinline__ long long iwc(const Geom& g, int i, int j, int k) {
+    return ((long long)k * g.ny + (j - 1)) * g.nx + (i - 1);
+}
+__device__ __forceinline__ long long icell(const Geom& g, int i, int j, int k) {
+    return ((long long)k * (g.ny + 2) + j) * (g.nx + 2) + i;
+}
+
+// rhs = div of the contravariant face velocities / dt (diver.f03:25-27)
+__global__ void k_diver(Geom g, const double* __restrict__ uc, const double* __restrict__ vc,
+                        const double* __restrict__ wc, double dt, double* __restrict__ b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    b[g.at(i, j, k)] = (uc[iuc(g, i, j, k)] - uc[iuc(g, i - 1, j, k)] + vc[ivc(g, i, j, k)] - vc[ivc(g, i, j - 1, k)] +
+                        wc[iwc(g, i, j, k)] - wc[iwc(g, i, j, k - 1)]) /
+                       dt;
+}
+
+// contravariant pressure gradient on the faces (gradie.f03:71-116) and the
+// face-velocity update of vel_up (uc: i = 0..jx; vc: j = 1..jy-1, the wall
+// faces keep their prescribed flux; wc: k = 0..jz).  The face gradients are
+// the face fluxes of the pressure operator at level 1 (A = g, B = g/4).
+__global__ void k_project_faces(Geom g, Coef<double> c, const double* __restrict__ x, double* __restrict__ uc,
+                                double* __restrict__ vc, double* __restrict__ wc, double dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long q = g.at(i, j, k);
+    if (j >= 1 && k >= 1) uc[iuc(g, i, j, k)] -= dt * flux_x(g, c, x, q);
+    if (i >= 1 && k >= 1 && j >= 1 && j <= g.ny - 1) vc[ivc(g, i, j, k)] -= dt * flux_y(g, c, x, q);
+    if (i >= 1 && j >= 1) wc[iwc(g, i, j, k)] -= dt * flux_z(g, c, x, q);
+}
+
+// Cartesian pressure gradient at the cell centres times -dt/2 J^-1
+// (gradie.f03:30-66) added to u, v, w (vel_up.f03:40-52), with the periodic
+// images in x and z
+struct Normals {
+    const double* p[9];  // csx, csy, csz, etx, ety, etz, ztx, zty, ztz boxes
+};
+__global__ void k_project_cells(Geom g, const double* __restrict__ x, Normals nrm, const double* __restrict__ giac,
+                                double* __restrict__ u, double* __restrict__ v, double* __restrict__ w, double dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const long long q = g.at(i, j, k), sj = g.sj, sk = g.sk;
+    const double coef = -0.5 * dt / giac[q];
+    const double f = x[q];
+    const double se = f + x[q + 1], sw = f + x[q - 1], sn = f + x[q + sj], ss = f + x[q - sj];
+    const double sf = f + x[q + sk], sb = f + x[q - sk];
+    double gr[3];
+    for (int d = 0; d < 3; ++d) {
+        const double* cs = nrm.p[d];
+        const double* et = nrm.p[3 + d];
+        const double* zt = nrm.p[6 + d];
+        gr[d] = coef * (cs[q] * se - cs[q - 1] * sw + et[q] * sn - et[q - sj] * ss + zt[q] * sf - zt[q - sk] * sb);
+    }
+    double* vel[3] = {u, v, w};
+    const int gi = i == g.nx ? 0 : (i == 1 ? g.nx + 1 : -1);
+    const int gk = k == g.nz ? 0 : (k == 1 ? g.nz + 1 : -1);
+    for (int d = 0; d < 3; ++d) {
+        double* a = vel[d];
+        const double nv = a[icell(g, i, j, k)] + gr[d];
+        a[icell(g, i, j, k)] = nv;
+        if (gi >= 0) a[icell(g, gi, j, k)] = nv;
+        if (gk >= 0) a[icell(g, i, j, gk)] = nv;
+        if (gi >= 0 && gk >= 0) a[icell(g, gi, j, gk)] = nv;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ples_mg_project(ples_mg_handle* h, double* uc, double* vc, double* wc, double* u, double* v, double* w,
+                    double* fi, double rel_tol, int max_cycles, ples_mg_stats* stats) {
+    if (!h || !uc || !vc || !wc || !fi || max_cycles < 0 || ((u || v || w) && !(u && v && w)))
+        return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        auto t0 = std::chrono::steady_clock::now();
+        const Geom& g = h->L[0].g;
+        const size_t nuc = (size_t)(g.nx + 1) * g.ny * g.nz, nvc = (size_t)g.nx * (g.ny + 1) * g.nz,
+                     nwc = (size_t)g.nx * g.ny * (g.nz + 1), ncell = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+        int rc;
+        if (!h->d_uc &&
+            ((rc = dalloc(h, (void**)&h->d_uc, 8 * nuc)) || (rc = dalloc(h, (void**)&h->d_vc, 8 * nvc)) ||
+             (rc = dalloc(h, (void**)&h->d_wc, 8 * nwc))))
+            return rc;
+        const bool cart = u != nullptr;
+        if (cart && !h->d_u) {
+            if ((rc = dalloc(h, (void**)&h->d_u, 8 * ncell)) || (rc = dalloc(h, (void**)&h->d_v, 8 * ncell)) ||
+                (rc = dalloc(h, (void**)&h->d_w, 8 * ncell)) || (rc = dalloc(h, (void**)&h->giac, 8 * (size_t)g.n)))
+                return rc;
+            for (int c = 0; c < 9; ++c)
+                if ((rc = dalloc(h, (void**)&h->nrm[c], 8 * (size_t)g.n))) return rc;
+            double* const nout[9] = {h->nrm[0], h->nrm[1], h->nrm[2], h->nrm[3], h->nrm[4],
+                                     h->nrm[5], h->nrm[6], h->nrm[7], h->nrm[8]};
+            const ples_mg_desc& d = h->d;
+            CK(launch_normals(h->xn, h->yn, h->zn, d.jx, d.jy, d.jz, d.ip, d.jp, d.kp, g, nout, h->giac, h->st));
+            h->launches += 4;
+        }
+        CK(cudaMemcpyAsync(h->d_uc, uc, 8 * nuc, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->d_vc, vc, 8 * nvc, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->d_wc, wc, 8 * nwc, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->fi_c, fi, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+        k_compact_to_box<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->fi_c, h->x);
+        const double dt = h->d.dt;
+        k_diver<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), dim3(32, 4), 0, h->st>>>(g, h->d_uc, h->d_vc,
+                                                                                       h->d_wc, dt, h->b);
+        h->launches += 2;
+        CK(cudaGetLastError());
+        if ((rc = upload_cs(h, nullptr, false))) return rc;
+        ples_mg_stats st{};
+        const int src = solve_any(h, rel_tol, 0.0, max_cycles, &st);
+        if (src != PLES_MG_OK && src != PLES_MG_NOT_CONVERGED && src != PLES_MG_DIVERGED) return src;
+        k_project_faces<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 1 + 3) / 4, g.nz + 1), dim3(32, 4), 0, h->st>>>(
+            g, h->L[0].cd, h->x, h->d_uc, h->d_vc, h->d_wc, dt);
+        ++h->launches;
+        if (cart) {
+            CK(cudaMemcpyAsync(h->d_u, u, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+            CK(cudaMemcpyAsync(h->d_v, v, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+            CK(cudaMemcpyAsync(h->d_w, w, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+            Normals pn;
+            for (int c = 0; c < 9; ++c) pn.p[c] = h->nrm[c];
+            k_project_cells<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), dim3(32, 4), 0, h->st>>>(
+                g, h->x, pn, h->giac, h->d_u, h->d_v, h->d_w, dt);
+            ++h->launches;
+            CK(cudaMemcpyAsync(u, h->d_u, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+            CK(cudaMemcpyAsync(v, h->d_v, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+            CK(cudaMemcpyAsync(w, h->d_w, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+        }
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(uc, h->d_uc, 8 * nuc, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(vc, h->d_vc, 8 * nvc, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(wc, h->d_wc, 8 * nwc, cudaMemcpyDeviceToHost, h->st));
+        k_box_to_compact<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->x, h->fi_c);
+        ++h->launches;
+        CK(cudaMemcpyAsync(fi, h->fi_c, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (stats) *stats = st;
+        return src;
+    });
+}
+
 // Autotuner: first the CTA width of the eta-line smoother per level (128 or
 // 256 threads; the kernel's own time, CUDA events), then the sweep count per
 // level and the V-cycles per outer iteration (time of whole solves to

@@ -69,7 +69,7 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_kernel_timing", "ples_mg_kernel_time", "ples_mg_batch_create",
            "ples_mg_batch_solve", "ples_mg_batch_solve_device", "ples_mg_batch_info",
            "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
-           "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune",
+           "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune", "ples_mg_project",
            "ples_mg_residual_norms_device")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
@@ -106,6 +106,7 @@ def load(build=True):
     L.ples_mg_kernel_time.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.ples_mg_residual_norms_device.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_double)]
     L.ples_mg_autotune.argtypes = [vp, vp, C.POINTER(Tuning)]
+    L.ples_mg_project.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
     L.ples_mg_batch_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
     L.ples_mg_batch_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
@@ -258,6 +259,23 @@ class Multigrid:
             self._h, C.c_void_p(int(d_fi)), C.c_void_p(int(d_rhs)), C.c_void_p(int(d_r) or None),
             C.c_void_p(int(stream) or None), out))
         return out[0], out[1]
+
+    def project(self, uc, vc, wc, fi, u=None, v=None, w=None, rel_tol=1e-10, max_cycles=200):
+        """Projection step (diver, solve, gradie, vel_up): returns the new
+        (uc, vc, wc, fi) and, if given, (u, v, w); inputs are not modified."""
+        jx, jy, jz = self.jx, self.jy, self.jz
+        shapes = [(jx + 1, jy, jz), (jx, jy + 1, jz), (jx, jy, jz + 1)] + [(jx + 2, jy + 2, jz + 2)] * 4
+        arrs = [None if a is None else _f64(a).copy(order="F") for a in (uc, vc, wc, fi, u, v, w)]
+        for a, sh in zip(arrs, shapes):
+            if a is not None and a.shape != sh:
+                raise ValueError(f"array of shape {a.shape}, expected {sh}")
+        ptr = [None if a is None else C.c_void_p(a.ctypes.data) for a in arrs]
+        st = Stats()
+        rc = self._L.ples_mg_project(self._h, ptr[0], ptr[1], ptr[2], ptr[4], ptr[5], ptr[6], ptr[3], rel_tol,
+                                     max_cycles, C.byref(st))
+        self._check(rc, allow=(OK, NOT_CONVERGED))
+        out = arrs[:4] + ([arrs[4], arrs[5], arrs[6]] if u is not None else [])
+        return out, st.as_dict()
 
     def autotune(self, rhs=None):
         """Time candidate smoother widths, sweep counts and inner cycles on
