@@ -34,7 +34,7 @@ def _rank(rank, world, port, times, out):
 
 def test_two_replicas_take_the_slowest_rank():
     times = [0.5, 0.8]
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.spawn(_rank, args=(2, _free_port(), times, out), nprocs=2, join=True)
     for r in range(2):
