@@ -173,6 +173,20 @@ int ples_mg_project(ples_mg_handle *h, double *uc, double *vc, double *wc, doubl
                     double *v, double *w, double *fi, double rel_tol, int max_cycles,
                     ples_mg_stats *stats);
 
+/* The whole pressure step: contra (fsrc/contra.f03:91-219, ip = kp = 0,
+ * jp = 1, potenziale = 0) and then the projection above.  On entry u,v,w are
+ * the intermediate Cartesian velocities with their ghost cells (the wall
+ * velocity in j = 0 and jy+1, periodic images in x and z) and uc,vc,wc the
+ * previous contravariant ones, of which only the wall faces vc(:,0,:),
+ * vc(:,jy,:) are read: the faces get the face-normal projection of the
+ * average of their two cells, the wall faces that of the wall velocity,
+ * and cs3/cs4 = new minus old wall flux drive the solve's wall condition.
+ * On return all six hold the projected velocities and fi the pressure.
+ * Replaces contra + diver + multi + gradie + vel_up
+ * (fsrc/stratiParticle.f03:2845-2937). */
+int ples_mg_step(ples_mg_handle *h, double *u, double *v, double *w, double *uc, double *vc,
+                 double *wc, double *fi, double rel_tol, int max_cycles, ples_mg_stats *stats);
+
 /* ---- autotuner ----------------------------------------------------------
  * No counterpart in the reference (its kss, nlevel and omega are fixed
  * inputs).  Times candidate settings on this handle's grid and keeps the

@@ -1,9 +1,12 @@
 """Projection step either side of the pressure solve: diver, gradie, vel_up.
 
-Test infrastructure: the oracle of ples_mg_project.  Restates, for a
-single domain with periodic x and z and walls in y (ip = kp = 0, jp = 1),
-potenziale = 0 and no free surface:
+Test infrastructure: the oracle of ples_mg_project and ples_mg_step.
+Restates, for a single domain with periodic x and z and walls in y
+(ip = kp = 0, jp = 1), potenziale = 0 and no free surface:
 
+* contra (fsrc/contra.f03:91-219): uc, vc, wc from the Cartesian u, v, w
+  averaged onto the faces, and the wall fluxes cs3, cs4 (new minus old vc
+  on the wall faces);
 * diver  (fsrc/diver.f03:25-27): rhs = div(uc, vc, wc) / dt;
 * gradie (fsrc/gradie.f03:30-116): the Cartesian pressure gradient at the
   cell centres times -dt/2 J^-1 from the face normals csx..ztz, and the
@@ -100,6 +103,33 @@ def face_normals(orc):
     ztz = z["xcsi"] * z["yeta"] - z["xeta"] * z["ycsi"]
     Jz = _jac(*(z[a + b] for b in ("csi", "eta", "zet") for a in "xyz"))
     return (csx, csy, csz, Jc), (etx, ety, etz, Je), (ztx, zty, ztz, Jz)
+
+
+def contra(orc, u, v, w, vc_old):
+    """Returns (uc, vc, wc, cs3, cs4) from the cell-centred u, v, w
+    (jx+2, jy+2, jz+2) and the previous vc, whose wall faces give the old
+    wall fluxes; cs3, cs4 are (jx, jz)."""
+    jx, jy, jz = orc.jx, orc.jy, orc.jz
+    (csx, csy, csz, _), (etx, ety, etz, _), (ztx, zty, ztz, _) = face_normals(orc)
+
+    def avg(a, s0, s1):
+        return .5 * (a[s0] + a[s1])
+
+    si0, si1 = np.s_[0:jx + 1, 1:jy + 1, 1:jz + 1], np.s_[1:jx + 2, 1:jy + 1, 1:jz + 1]
+    uc = avg(u, si0, si1) * csx + avg(v, si0, si1) * csy + avg(w, si0, si1) * csz
+    vc = np.empty((jx, jy + 1, jz))
+    sj0, sj1 = np.s_[1:jx + 1, 1:jy, 1:jz + 1], np.s_[1:jx + 1, 2:jy + 1, 1:jz + 1]
+    vc[:, 1:jy] = (avg(u, sj0, sj1) * etx[:, 1:jy] + avg(v, sj0, sj1) * ety[:, 1:jy]
+                   + avg(w, sj0, sj1) * etz[:, 1:jy])
+    cs = []
+    for jf, jw in ((0, 0), (jy, jy + 1)):
+        flux = (u[1:jx + 1, jw, 1:jz + 1] * etx[:, jf] + v[1:jx + 1, jw, 1:jz + 1] * ety[:, jf]
+                + w[1:jx + 1, jw, 1:jz + 1] * etz[:, jf])
+        cs.append(flux - vc_old[:, jf])
+        vc[:, jf] = flux
+    sk0, sk1 = np.s_[1:jx + 1, 1:jy + 1, 0:jz + 1], np.s_[1:jx + 1, 1:jy + 1, 1:jz + 2]
+    wc = avg(u, sk0, sk1) * ztx + avg(v, sk0, sk1) * zty + avg(w, sk0, sk1) * ztz
+    return uc, vc, wc, cs[0], cs[1]
 
 
 def diver(uc, vc, wc, dt):

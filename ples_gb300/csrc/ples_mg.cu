@@ -1555,6 +1555,128 @@ __global__ void k_project_cells(Geom g, const double* __restrict__ x, Normals nr
     }
 }
 
+// intermediate contravariant velocities from the Cartesian ones and the
+// wall fluxes cs3/cs4 (contra.f03:31-200 with ip = kp = 0, jp = 1,
+// potenziale = 0): interior faces get the face-normal projection of the
+// average of their two cells; the wall faces get that of the wall velocity
+// (the ghost cell), and cs = new wall flux - old wall flux
+__global__ void k_contra(Geom g, Normals nrm, const double* __restrict__ u, const double* __restrict__ v,
+                         const double* __restrict__ w, double* __restrict__ uc, double* __restrict__ vc,
+                         double* __restrict__ wc, double* __restrict__ cs3, double* __restrict__ cs4) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const long long q = g.at(i, j, k);
+    auto C = [&](const double* a, int ii, int jj, int kk) { return a[icell(g, ii, jj, kk)]; };
+    if (j >= 1 && k >= 1) {  // csi face i = 0..jx
+        const double ui = .5 * (C(u, i, j, k) + C(u, i + 1, j, k)), vi = .5 * (C(v, i, j, k) + C(v, i + 1, j, k)),
+                     wi = .5 * (C(w, i, j, k) + C(w, i + 1, j, k));
+        uc[iuc(g, i, j, k)] = ui * nrm.p[0][q] + vi * nrm.p[1][q] + wi * nrm.p[2][q];
+    }
+    if (i >= 1 && k >= 1) {  // eta face j = 0..jy
+        const long long qv = ivc(g, i, j, k);
+        if (j >= 1 && j <= g.ny - 1) {
+            const double ui = .5 * (C(u, i, j, k) + C(u, i, j + 1, k)), vi = .5 * (C(v, i, j, k) + C(v, i, j + 1, k)),
+                         wi = .5 * (C(w, i, j, k) + C(w, i, j + 1, k));
+            vc[qv] = ui * nrm.p[3][q] + vi * nrm.p[4][q] + wi * nrm.p[5][q];
+        } else {
+            const int jw = j == 0 ? 0 : g.ny + 1;  // the wall velocity in the ghost row
+            const double flux = C(u, i, jw, k) * nrm.p[3][q] + C(v, i, jw, k) * nrm.p[4][q] + C(w, i, jw, k) * nrm.p[5][q];
+            double* cs = j == 0 ? cs3 : cs4;
+            cs[(long long)(k - 1) * g.nx + (i - 1)] = flux - vc[qv];
+            vc[qv] = flux;
+        }
+    }
+    if (i >= 1 && j >= 1) {  // zeta face k = 0..jz
+        const double ui = .5 * (C(u, i, j, k) + C(u, i, j, k + 1)), vi = .5 * (C(v, i, j, k) + C(v, i, j, k + 1)),
+                     wi = .5 * (C(w, i, j, k) + C(w, i, j, k + 1));
+        wc[iwc(g, i, j, k)] = ui * nrm.p[6][q] + vi * nrm.p[7][q] + wi * nrm.p[8][q];
+    }
+}
+
+// The projection step, optionally preceded by contra (with_contra: u,v,w
+// are the intermediate Cartesian velocities, uc,vc,wc the previous
+// contravariant ones, of which the wall faces of vc are read).
+int project_core(ples_mg_handle* h, double* uc, double* vc, double* wc, double* u, double* v, double* w, double* fi,
+                 double rel_tol, int max_cycles, ples_mg_stats* stats, bool with_contra) {
+    auto t0 = std::chrono::steady_clock::now();
+    const Geom& g = h->L[0].g;
+    const size_t nuc = (size_t)(g.nx + 1) * g.ny * g.nz, nvc = (size_t)g.nx * (g.ny + 1) * g.nz,
+                 nwc = (size_t)g.nx * g.ny * (g.nz + 1), ncell = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+    int rc;
+    if (!h->d_uc &&
+        ((rc = dalloc(h, (void**)&h->d_uc, 8 * nuc)) || (rc = dalloc(h, (void**)&h->d_vc, 8 * nvc)) ||
+         (rc = dalloc(h, (void**)&h->d_wc, 8 * nwc))))
+        return rc;
+    const bool cart = u != nullptr;
+    if (cart && !h->d_u) {
+        if ((rc = dalloc(h, (void**)&h->d_u, 8 * ncell)) || (rc = dalloc(h, (void**)&h->d_v, 8 * ncell)) ||
+            (rc = dalloc(h, (void**)&h->d_w, 8 * ncell)) || (rc = dalloc(h, (void**)&h->giac, 8 * (size_t)g.n)))
+            return rc;
+        for (int c = 0; c < 9; ++c)
+            if ((rc = dalloc(h, (void**)&h->nrm[c], 8 * (size_t)g.n))) return rc;
+        double* const nout[9] = {h->nrm[0], h->nrm[1], h->nrm[2], h->nrm[3], h->nrm[4],
+                                 h->nrm[5], h->nrm[6], h->nrm[7], h->nrm[8]};
+        const ples_mg_desc& d = h->d;
+        CK(launch_normals(h->xn, h->yn, h->zn, d.jx, d.jy, d.jz, d.ip, d.jp, d.kp, g, nout, h->giac, h->st));
+        h->launches += 4;
+    }
+    Normals pn;
+    for (int c = 0; c < 9; ++c) pn.p[c] = h->nrm[c];
+    CK(cudaMemcpyAsync(h->d_uc, uc, 8 * nuc, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_vc, vc, 8 * nvc, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_wc, wc, 8 * nwc, cudaMemcpyHostToDevice, h->st));
+    if (cart) {
+        CK(cudaMemcpyAsync(h->d_u, u, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->d_v, v, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->d_w, w, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+    }
+    CK(cudaMemcpyAsync(h->fi_c, fi, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+    k_compact_to_box<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->fi_c, h->x);
+    ++h->launches;
+    if (with_contra) {
+        for (int s = 2; s <= 3; ++s)
+            if (!h->cs_buf[s] && (rc = dalloc(h, (void**)&h->cs_buf[s], 8 * (size_t)g.nx * g.nz))) return rc;
+        k_contra<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 1 + 3) / 4, g.nz + 1), dim3(32, 4), 0, h->st>>>(
+            g, pn, h->d_u, h->d_v, h->d_w, h->d_uc, h->d_vc, h->d_wc, h->cs_buf[2], h->cs_buf[3]);
+        ++h->launches;
+        for (int s = 0; s < 6; ++s) h->cs_c[s] = (s == 2 || s == 3) ? h->cs_buf[s] : nullptr;
+    } else if ((rc = upload_cs(h, nullptr, false))) {
+        return rc;
+    }
+    const double dt = h->d.dt;
+    k_diver<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), dim3(32, 4), 0, h->st>>>(g, h->d_uc, h->d_vc, h->d_wc,
+                                                                                   dt, h->b);
+    ++h->launches;
+    CK(cudaGetLastError());
+    ples_mg_stats st{};
+    const int src = solve_any(h, rel_tol, 0.0, max_cycles, &st);
+    if (src != PLES_MG_OK && src != PLES_MG_NOT_CONVERGED && src != PLES_MG_DIVERGED) return src;
+    k_project_faces<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 1 + 3) / 4, g.nz + 1), dim3(32, 4), 0, h->st>>>(
+        g, h->L[0].cd, h->x, h->d_uc, h->d_vc, h->d_wc, dt);
+    ++h->launches;
+    if (cart) {
+        k_project_cells<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), dim3(32, 4), 0, h->st>>>(
+            g, h->x, pn, h->giac, h->d_u, h->d_v, h->d_w, dt);
+        ++h->launches;
+        CK(cudaMemcpyAsync(u, h->d_u, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(v, h->d_v, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(w, h->d_w, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(uc, h->d_uc, 8 * nuc, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(vc, h->d_vc, 8 * nvc, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(wc, h->d_wc, 8 * nwc, cudaMemcpyDeviceToHost, h->st));
+    k_box_to_compact<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->x, h->fi_c);
+    ++h->launches;
+    CK(cudaMemcpyAsync(fi, h->fi_c, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = st;
+    return src;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1564,69 +1686,16 @@ int ples_mg_project(ples_mg_handle* h, double* uc, double* vc, double* wc, doubl
     if (!h || !uc || !vc || !wc || !fi || max_cycles < 0 || ((u || v || w) && !(u && v && w)))
         return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
     return with_device(h, [&]() -> int {
-        auto t0 = std::chrono::steady_clock::now();
-        const Geom& g = h->L[0].g;
-        const size_t nuc = (size_t)(g.nx + 1) * g.ny * g.nz, nvc = (size_t)g.nx * (g.ny + 1) * g.nz,
-                     nwc = (size_t)g.nx * g.ny * (g.nz + 1), ncell = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
-        int rc;
-        if (!h->d_uc &&
-            ((rc = dalloc(h, (void**)&h->d_uc, 8 * nuc)) || (rc = dalloc(h, (void**)&h->d_vc, 8 * nvc)) ||
-             (rc = dalloc(h, (void**)&h->d_wc, 8 * nwc))))
-            return rc;
-        const bool cart = u != nullptr;
-        if (cart && !h->d_u) {
-            if ((rc = dalloc(h, (void**)&h->d_u, 8 * ncell)) || (rc = dalloc(h, (void**)&h->d_v, 8 * ncell)) ||
-                (rc = dalloc(h, (void**)&h->d_w, 8 * ncell)) || (rc = dalloc(h, (void**)&h->giac, 8 * (size_t)g.n)))
-                return rc;
-            for (int c = 0; c < 9; ++c)
-                if ((rc = dalloc(h, (void**)&h->nrm[c], 8 * (size_t)g.n))) return rc;
-            double* const nout[9] = {h->nrm[0], h->nrm[1], h->nrm[2], h->nrm[3], h->nrm[4],
-                                     h->nrm[5], h->nrm[6], h->nrm[7], h->nrm[8]};
-            const ples_mg_desc& d = h->d;
-            CK(launch_normals(h->xn, h->yn, h->zn, d.jx, d.jy, d.jz, d.ip, d.jp, d.kp, g, nout, h->giac, h->st));
-            h->launches += 4;
-        }
-        CK(cudaMemcpyAsync(h->d_uc, uc, 8 * nuc, cudaMemcpyHostToDevice, h->st));
-        CK(cudaMemcpyAsync(h->d_vc, vc, 8 * nvc, cudaMemcpyHostToDevice, h->st));
-        CK(cudaMemcpyAsync(h->d_wc, wc, 8 * nwc, cudaMemcpyHostToDevice, h->st));
-        CK(cudaMemcpyAsync(h->fi_c, fi, 8 * ncell, cudaMemcpyHostToDevice, h->st));
-        k_compact_to_box<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->fi_c, h->x);
-        const double dt = h->d.dt;
-        k_diver<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), dim3(32, 4), 0, h->st>>>(g, h->d_uc, h->d_vc,
-                                                                                       h->d_wc, dt, h->b);
-        h->launches += 2;
-        CK(cudaGetLastError());
-        if ((rc = upload_cs(h, nullptr, false))) return rc;
-        ples_mg_stats st{};
-        const int src = solve_any(h, rel_tol, 0.0, max_cycles, &st);
-        if (src != PLES_MG_OK && src != PLES_MG_NOT_CONVERGED && src != PLES_MG_DIVERGED) return src;
-        k_project_faces<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 1 + 3) / 4, g.nz + 1), dim3(32, 4), 0, h->st>>>(
-            g, h->L[0].cd, h->x, h->d_uc, h->d_vc, h->d_wc, dt);
-        ++h->launches;
-        if (cart) {
-            CK(cudaMemcpyAsync(h->d_u, u, 8 * ncell, cudaMemcpyHostToDevice, h->st));
-            CK(cudaMemcpyAsync(h->d_v, v, 8 * ncell, cudaMemcpyHostToDevice, h->st));
-            CK(cudaMemcpyAsync(h->d_w, w, 8 * ncell, cudaMemcpyHostToDevice, h->st));
-            Normals pn;
-            for (int c = 0; c < 9; ++c) pn.p[c] = h->nrm[c];
-            k_project_cells<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), dim3(32, 4), 0, h->st>>>(
-                g, h->x, pn, h->giac, h->d_u, h->d_v, h->d_w, dt);
-            ++h->launches;
-            CK(cudaMemcpyAsync(u, h->d_u, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
-            CK(cudaMemcpyAsync(v, h->d_v, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
-            CK(cudaMemcpyAsync(w, h->d_w, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
-        }
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(uc, h->d_uc, 8 * nuc, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(vc, h->d_vc, 8 * nvc, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(wc, h->d_wc, 8 * nwc, cudaMemcpyDeviceToHost, h->st));
-        k_box_to_compact<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->x, h->fi_c);
-        ++h->launches;
-        CK(cudaMemcpyAsync(fi, h->fi_c, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaStreamSynchronize(h->st));
-        st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if (stats) *stats = st;
-        return src;
+        return project_core(h, uc, vc, wc, u, v, w, fi, rel_tol, max_cycles, stats, false);
+    });
+}
+
+int ples_mg_step(ples_mg_handle* h, double* u, double* v, double* w, double* uc, double* vc, double* wc, double* fi,
+                 double rel_tol, int max_cycles, ples_mg_stats* stats) {
+    if (!h || !u || !v || !w || !uc || !vc || !wc || !fi || max_cycles < 0)
+        return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    return with_device(h, [&]() -> int {
+        return project_core(h, uc, vc, wc, u, v, w, fi, rel_tol, max_cycles, stats, true);
     });
 }
 

@@ -70,7 +70,7 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_batch_solve", "ples_mg_batch_solve_device", "ples_mg_batch_info",
            "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
            "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune", "ples_mg_project",
-           "ples_mg_residual_norms_device")
+           "ples_mg_step", "ples_mg_residual_norms_device")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -107,6 +107,7 @@ def load(build=True):
     L.ples_mg_residual_norms_device.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_double)]
     L.ples_mg_autotune.argtypes = [vp, vp, C.POINTER(Tuning)]
     L.ples_mg_project.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
+    L.ples_mg_step.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
     L.ples_mg_batch_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
     L.ples_mg_batch_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
@@ -276,6 +277,23 @@ class Multigrid:
         self._check(rc, allow=(OK, NOT_CONVERGED))
         out = arrs[:4] + ([arrs[4], arrs[5], arrs[6]] if u is not None else [])
         return out, st.as_dict()
+
+    def step(self, u, v, w, uc, vc, wc, fi, rel_tol=1e-10, max_cycles=200):
+        """The pressure step from the intermediate Cartesian velocities
+        (contra, diver, solve, gradie, vel_up): returns the new
+        (u, v, w, uc, vc, wc, fi); inputs are not modified."""
+        jx, jy, jz = self.jx, self.jy, self.jz
+        cell = (jx + 2, jy + 2, jz + 2)
+        shapes = [cell] * 3 + [(jx + 1, jy, jz), (jx, jy + 1, jz), (jx, jy, jz + 1), cell]
+        arrs = [_f64(a).copy(order="F") for a in (u, v, w, uc, vc, wc, fi)]
+        for a, sh in zip(arrs, shapes):
+            if a.shape != sh:
+                raise ValueError(f"array of shape {a.shape}, expected {sh}")
+        st = Stats()
+        rc = self._L.ples_mg_step(self._h, *[C.c_void_p(a.ctypes.data) for a in arrs], rel_tol, max_cycles,
+                                  C.byref(st))
+        self._check(rc, allow=(OK, NOT_CONVERGED))
+        return arrs, st.as_dict()
 
     def autotune(self, rhs=None):
         """Time candidate smoother widths, sweep counts and inner cycles on
