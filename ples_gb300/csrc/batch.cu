@@ -320,7 +320,7 @@ struct Builder {
     }
 };
 
-dim3 line_grid(const Geom& g) { return dim3((g.nz + 1) / 2, (g.nx + 31) / 32, 1); }
+dim3 line_grid(const Geom& g) { return dim3((g.nx + 31) / 32, (g.nz + 1) / 2, 1); }
 dim3 rr_grid(const Geom& gc) { return dim3((gc.nx + 31) / 32, (gc.ny + 3) / 4, gc.nz); }
 dim3 prol_grid(const Geom& gf, const Geom& gc) { return dim3((gc.nx + 1 + 31) / 32, (gf.ny + 2 + 3) / 4, gf.nz + 2); }
 dim3 box_grid2(const Geom& g) { return dim3((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2); }

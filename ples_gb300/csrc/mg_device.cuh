@@ -85,10 +85,23 @@ __device__ __forceinline__ Blk hw_blk() {
 
 template <typename T>
 __device__ __forceinline__ T ld(const T* p, long long q) { return __ldg(p + q); }
+template <typename T>
+__device__ __forceinline__ T ld(const T* p, unsigned q) { return __ldg(p + q); }
+
+// element offset of (i,j,k) in 32 bits: a box has fewer than 2^31 elements
+// (checked when a handle is created), so kernels that issue many loads per
+// cell form each address with one 32x32->64 multiply-add
+__device__ __forceinline__ unsigned at32(const Geom& g, int i, int j, int k) {
+    return (unsigned)k * (unsigned)g.sk + (unsigned)j * (unsigned)g.sj + (unsigned)(i + kOX);
+}
 
 // hint the L2 to fetch the line holding p[q] (no register, no L1 allocation)
 template <typename T>
 __device__ __forceinline__ void pf_l2(const T* p, long long q) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + q));
+}
+template <typename T>
+__device__ __forceinline__ void pf_l2(const T* p, unsigned q) {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p + q));
 }
 
@@ -378,6 +391,290 @@ __device__ __forceinline__ void odd_x_terms(const Geom& g, const Coef<T>& c, con
     }
 }
 
+// the values of the lane beside (i-1 / i+1); lanes 0 and 31 take the column
+// just outside the tile, h, which they loaded themselves
+template <typename T>
+__device__ __forceinline__ T from_west(T v, T h) {
+    const T s = __shfl_up_sync(0xffffffffu, v, 1);
+    return (threadIdx.x & 31) == 0 ? h : s;
+}
+template <typename T>
+__device__ __forceinline__ T from_east(T v, T h) {
+    const T s = __shfl_down_sync(0xffffffffu, v, 1);
+    return (threadIdx.x & 31) == 31 ? h : s;
+}
+
+// Phase 1 of the plain-load smoother: warp w builds the rows of its own
+// segment j0..j1-1 (the one seg_thomas gives it) in order.  The pressure
+// rows j-1, j, j+1 of planes k-1, k, k+1 stay in a three-row window and the
+// eta-face coefficients of row j-1 are carried, so a step loads one new
+// pressure row per plane and the coefficients of row j once; the i-1 / i+1
+// values come from the lanes beside, and lanes 0 and 31 load the columns
+// just outside the tile.  Every lane up to the east ghost column i = nx+1
+// holds its pressure column; the rows and the arithmetic of each equation
+// are those of the strided form (same expressions, same order).
+// Loads ahead: rows PLES_LINE_PF_ROWS further on are hinted into L2.
+template <typename T, bool ZEBRA, bool ZIN>
+__device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, const T* __restrict__ cpa,
+                                           const T* __restrict__ pin, const T* __restrict__ pk,
+                                           const T* __restrict__ rh, T omega, int zk, int i, int k, bool odd, T* G,
+                                           T* AL, T* CP) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nj = g.ny + 2, ny = g.ny;
+    const int len = (nj + nw - 1) / nw;
+    const int j0 = min(w * len, nj), j1 = min(j0 + len, nj);
+    const unsigned sj = (unsigned)g.sj, sk = (unsigned)g.sk;
+    const bool act = i <= g.nx;      // the lane owns a line
+    const bool col = i <= g.nx + 1;  // the lane holds a pressure column (the last may be the ghost)
+    const bool halo = lane == 0 || (lane == 31 && i + 1 <= g.nx + 1);
+    const int hd = lane == 0 ? -1 : 1;
+    const bool noneigh = ZIN && (!ZEBRA || zk);  // every old neighbour is zero
+    const bool kz = zk || noneigh;               // the k+-1 planes are zero
+    auto row = [&](const T* a, int j, unsigned qk, T& v, T& h) {  // qk: offset of (i, 0, plane)
+        v = T(0);
+        h = T(0);
+        if (j < 0 || j > ny + 1) return;
+        const unsigned q = qk + (unsigned)j * sj;
+        if (col) v = ld(a, q);
+        if (halo) h = ld(a, q + hd);
+    };
+    const unsigned q0 = at32(g, i, 0, k);
+    // window: plane k (P), k+1 (F), k-1 (B); rows j-1 (m), j (0), j+1 (p);
+    // h* the halo column of lanes 0 / 31; E*/W* the east / west values of
+    // plane k (shuffled once per row and carried)
+    T Pm = T(0), P0 = T(0), Pp = T(0);
+    T EPm = T(0), EP0 = T(0), EPp = T(0), WPm = T(0), WP0 = T(0), WPp = T(0);
+    T Fm = T(0), F0 = T(0), Fp = T(0), hF0 = T(0), hFp = T(0);
+    T Bm = T(0), B0 = T(0), Bp = T(0), hB0 = T(0), hBp = T(0);
+    if (j0 >= j1) return;
+    if (!ZIN) {
+        T hP0, hPp;
+        row(pin, j0 - 1, q0, P0, hP0);
+        row(pin, j0, q0, Pp, hPp);
+        EP0 = from_east(P0, hP0);
+        WP0 = from_west(P0, hP0);
+        EPp = from_east(Pp, hPp);
+        WPp = from_west(Pp, hPp);
+    }
+    if (!kz) {
+        T d0, d1;
+        row(pk, j0 - 1, q0 + sk, F0, d0);
+        row(pk, j0, q0 + sk, Fp, hFp);
+        row(pk, j0 - 1, q0 - sk, B0, d1);
+        row(pk, j0, q0 - sk, Bp, hBp);
+    }
+    // eta-face coefficients of row j-1 (a2, b21, b23) and its LU factor c'
+    T a2s = T(0), b21s = T(0), b23s = T(0), cps = T(0);
+    if (act && j0 >= 1) {
+        const unsigned q = q0 + (unsigned)(j0 - 1) * sj;
+        a2s = ld(c.a2, q);
+        b21s = ld(c.b21, q);
+        b23s = ld(c.b23, q);
+        cps = ld(cpa, q);
+    }
+    for (int j = j0; j < j1; ++j) {
+        const unsigned q = q0 + (unsigned)j * sj;
+        // every load of the step first: the coefficients of row j ...
+        T a2v = T(0), b21v = T(0), b23v = T(0), cpv = T(0);
+        T a1e = T(0), b12v = T(0), b13v = T(0), a1h = T(0), b12h = T(0), b13h = T(0);
+        T a3f = T(0), a3b = T(0), b31v = T(0), b31b = T(0), b32v = T(0), b32b = T(0), rhv = T(0);
+        if (act && j <= ny) {
+            a2v = ld(c.a2, q);
+            b21v = ld(c.b21, q);
+            b23v = ld(c.b23, q);
+            cpv = ld(cpa, q);
+        }
+        if (act && j >= 1 && j <= ny) {
+            a1e = ld(c.a1, q); b12v = ld(c.b12, q); b13v = ld(c.b13, q);
+            a3f = ld(c.a3, q); b31v = ld(c.b31, q); b32v = ld(c.b32, q);
+            a3b = ld(c.a3, q - sk); b31b = ld(c.b31, q - sk); b32b = ld(c.b32, q - sk);
+            rhv = ld(rh, q);
+            if (lane == 0) { a1h = ld(c.a1, q - 1); b12h = ld(c.b12, q - 1); b13h = ld(c.b13, q - 1); }
+        }
+        // ... then the pressure rows j+1 of the three planes
+        Pm = P0; P0 = Pp;
+        EPm = EP0; EP0 = EPp; WPm = WP0; WP0 = WPp;
+        Fm = F0; F0 = Fp; hF0 = hFp;
+        Bm = B0; B0 = Bp; hB0 = hBp;
+        T hPp = T(0);
+        if (!ZIN) row(pin, j + 1, q0, Pp, hPp);
+        if (!kz) {
+            row(pk, j + 1, q0 + sk, Fp, hFp);
+            row(pk, j + 1, q0 - sk, Bp, hBp);
+        }
+#if PLES_LINE_PF_ROWS > 0
+        if (act && j + PLES_LINE_PF_ROWS < j1) {
+            const unsigned qn = q + PLES_LINE_PF_ROWS * sj;
+            pf_l2(c.a1, qn); pf_l2(c.b12, qn); pf_l2(c.b13, qn);
+            pf_l2(c.a2, qn); pf_l2(c.b21, qn); pf_l2(c.b23, qn);
+            pf_l2(c.a3, qn); pf_l2(c.b31, qn); pf_l2(c.b32, qn);
+            pf_l2(c.a3, qn - sk); pf_l2(c.b31, qn - sk); pf_l2(c.b32, qn - sk);
+            pf_l2(rh, qn); pf_l2(cpa, qn);
+            if (!ZIN) pf_l2(pin, qn + sj);
+            if (!kz) { pf_l2(pk, qn + sj + sk); pf_l2(pk, qn + sj - sk); }
+        }
+#endif
+        if (!ZIN) {
+            EPp = from_east(Pp, hPp);
+            WPp = from_west(Pp, hPp);
+        }
+        // the in-plane x-neighbours
+        const T pe = EP0, pw = WP0, pes = EPm, pws = WPm, pen = EPp, pwn = WPp;
+        T f = T(0), a = T(0), im = T(1), tp = T(0);  // tp = (T p_old)(j), T the line operator
+        if (j == 0) {
+            if (act) {
+                f = noneigh ? T(0) : b23v * (Fp + F0 - Bp - B0);
+                if (!odd && !noneigh) f += b21v * (pen + pe - pwn - pw);
+                a = T(0);
+                im = T(1) / a2v;
+                tp = a2v * P0 - a2v * Pp;
+                if (a2v == T(0)) { im = T(1); f = T(0); tp = P0; }  // wall row above a solid cell
+            }
+        } else if (j == ny + 1) {
+            if (act) {
+                f = noneigh ? T(0) : -(b23s * (F0 + Fm - B0 - Bm));
+                if (!odd && !noneigh) f -= b21s * (pe + pes - pw - pws);
+                a = -a2s;
+                im = T(1) / (a2s - a * cps);
+                tp = a2s * P0 - a2s * Pm;
+                if (a2s == T(0)) { im = T(1); f = T(0); tp = P0; }  // wall row below a solid cell
+            }
+        } else {
+            const T a1w = from_west(a1e, a1h), b12w = from_west(b12v, b12h), b13w = from_west(b13v, b13h);
+            const T pef = from_east(F0, hF0), pwf = from_west(F0, hF0);
+            const T peb = from_east(B0, hB0), pwb = from_west(B0, hB0);
+            if (act) {
+                a = a2s;
+                const T b = -(a2v + a + a1e + a1w + a3f + a3b);
+                im = T(1) / (b - a * cps);
+                f = rhv;
+                tp = a * Pm + b * P0 + a2v * Pp;
+                if (b == T(0)) {  // solid cell of an immersed-boundary mask: identity row
+                    im = T(1);
+                    f = T(0);
+                    a = T(0);
+                    tp = P0;
+                }
+                if (!noneigh) {
+                    const T pn = Pp, ps = Pm, pf = F0, pb = B0;
+                    const T pnf = Fp, pnb = Bp, psf = Fm, psb = Bm;
+                    // every term without an in-plane x-neighbour
+                    T rest = a3f * pf + a3b * pb + (b12v - b12w) * (pn - ps);
+                    rest += b13v * (pef + pf - peb - pb) - b13w * (pf + pwf - pb - pwb);
+                    rest += b23v * (pnf + pf - pnb - pb) - b23s * (pf + psf - pb - psb);
+                    rest += b31v * (pef - pwf) - b31b * (peb - pwb);
+                    rest += b32v * (pnf + pn - psf - ps) - b32b * (pn + pnb - ps - psb);
+                    f -= rest;
+                    if (!odd) {  // the in-plane x-neighbour terms, old values
+                        const T tx = a1e * pe + a1w * pw + b12v * (pen - pes) - b12w * (pwn - pws) +
+                                     b21v * (pen + pe - pwn - pw) - b21s * (pe + pes - pw - pws) +
+                                     (b31v - b31b) * (pe - pw);
+                        f -= tx;
+                    }
+                }
+            }
+        }
+        if (act) {
+            // the over-relaxation folded into the right-hand side: with T the
+            // line operator of row j, T x = omega f + (1 - omega) T p_old
+            // gives x = p_old + omega (T^-1 f - p_old) (identity rows keep
+            // T p_old = p_old)
+            G[j * 32 + lane] = (ZIN ? omega * f : omega * f + (T(1) - omega) * tp) * im;
+            AL[j * 32 + lane] = a * im;
+            // odd lanes keep 1/m here until their x-neighbour terms are added
+            CP[j * 32 + lane] = odd ? im : (j == ny + 1 ? T(0) : cpv);
+        }
+        a2s = a2v; b21s = b21v; b23s = b23v; cps = cpv;
+    }
+}
+
+// Zebra second half, plain-load form of odd_x_terms: warp w adds the x-
+// neighbour terms to the rows of its own segment, kXR consecutive rows per
+// batch with every load of a batch issued first.  The even lanes load a1 and
+// b12 for the odd lanes east of them (shuffled across), lane 0 the column
+// i0-1 outside the tile (its old pressure rows and the two coefficients),
+// and b21 of row j-1 is carried from the previous row.
+template <typename T, bool ZIN>
+__device__ __forceinline__ void odd_x_rows(const Geom& g, const Coef<T>& c, const T* __restrict__ cpa,
+                                           const T* __restrict__ pin, T omega, T* G, T* CP, int i, int k) {
+    constexpr int kXR = 2;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nj = g.ny + 2, ny = g.ny;
+    const int len = (nj + nw - 1) / nw;
+    const int j0 = min(w * len, nj), j1 = min(j0 + len, nj);
+    const unsigned sj = (unsigned)g.sj, sk = (unsigned)g.sk, q0 = at32(g, i, 0, k);
+    const bool act = i <= g.nx;
+    const bool mine = act && (i & 1);
+    const bool east_in = i + 1 <= g.nx;  // i+1 is a lane of this tile (odd lanes are never lane 31)
+    // the new value of the east / west neighbour at row jj (old field outside the tile)
+    auto EV = [&](int jj) -> T {
+        if (east_in) return G[jj * 32 + lane + 1];
+        return ZIN ? T(0) : ld(pin, q0 + (unsigned)jj * sj + 1u);
+    };
+    T b21c = T(0);  // b21 of the row before the batch
+    if (mine && j0 >= 1 && j0 < j1) b21c = ld(c.b21, q0 + (unsigned)(j0 - 1) * sj);
+    for (int jb = j0; jb < j1; jb += kXR) {
+        T a1[kXR], a1h[kXR], b12[kXR], b12h[kXR], b21[kXR], b31[kXR], b31b[kXR], cpv[kXR], wv[kXR + 2];
+#pragma unroll
+        for (int u = 0; u < kXR; ++u) {
+            const int j = min(jb + u, j1 - 1);
+            const unsigned q = q0 + (unsigned)j * sj;
+            a1[u] = act ? ld(c.a1, q) : T(0);
+            b12[u] = act ? ld(c.b12, q) : T(0);
+            a1h[u] = act && lane == 0 ? ld(c.a1, q - 1) : T(0);
+            b12h[u] = act && lane == 0 ? ld(c.b12, q - 1) : T(0);
+            b21[u] = mine ? ld(c.b21, q) : T(0);
+            b31[u] = mine ? ld(c.b31, q) : T(0);
+            b31b[u] = mine ? ld(c.b31, q - sk) : T(0);
+            cpv[u] = mine ? ld(cpa, q) : T(0);
+        }
+#pragma unroll
+        for (int v = 0; v < kXR + 2; ++v) {  // old west column, rows jb-1 .. jb+kXR
+            const int jj = jb - 1 + v;
+            wv[v] = !ZIN && act && lane == 0 && jj >= 0 && jj <= ny + 1 ? ld(pin, q0 + (unsigned)jj * sj - 1u) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kXR; ++u) {
+            const int j = jb + u;
+            if (j >= j1) break;
+            const T a1w = from_west(a1[u], a1h[u]);
+            const T b12w = from_west(b12[u], b12h[u]);
+            const T b21s = u == 0 ? b21c : b21[u - 1];
+            if (mine) {
+                const bool l0 = lane == 0;
+                const T pw = l0 ? wv[u + 1] : G[j * 32 + lane - 1];
+                const T pwn = j < nj - 1 ? (l0 ? wv[u + 2] : G[(j + 1) * 32 + lane - 1]) : T(0);
+                const T pws = j > 0 ? (l0 ? wv[u] : G[(j - 1) * 32 + lane - 1]) : T(0);
+                const T pe = EV(j);
+                T tx;
+                if (j == 0) {
+                    tx = -b21[u] * (EV(j + 1) + pe - pwn - pw);
+                } else if (j == ny + 1) {
+                    tx = b21s * (pe + EV(j - 1) - pw - pws);
+                } else {
+                    const T pen = EV(j + 1), pes = EV(j - 1);
+                    tx = a1[u] * pe + a1w * pw + b12[u] * (pen - pes) - b12w * (pwn - pws) +
+                         b21[u] * (pen + pe - pwn - pw) - b21s * (pe + pes - pw - pws) + (b31[u] - b31b[u]) * (pe - pw);
+                }
+                const T im = CP[j * 32 + lane];
+                G[j * 32 + lane] -= omega * tx * im;
+                CP[j * 32 + lane] = j == ny + 1 ? T(0) : cpv[u];
+            }
+        }
+        b21c = b21[kXR - 1];
+    }
+}
+
+// Phase 3 when the relaxation is folded into the right-hand side (the
+// plain-load smoother): G already holds the new values; store the rows
+// j = w, w+nw, ... with their periodic images.
+template <typename T>
+__device__ __forceinline__ void store_rows(const Geom& g, T* pout, const T* G, int i, int k) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nj = g.ny + 2;
+    for (int j = w; j < nj; j += nw) store_periodic(g, pout, i, j, k, G[j * 32 + lane]);
+}
+
 // Phase 3: relax the rows j = w, w+nw, ... of this lane's line, keep the
 // new value in G (zebra: the odd-i lines read it) and store it with its
 // periodic images.  The old values of a batch of kRB rows are loaded first.
@@ -410,12 +707,15 @@ __device__ __forceinline__ void relax_store(const Geom& g, const T* __restrict__
 // eta-line relaxation (the device form of solut_sndrcv_slor,
 // multigrid.f03:1939-2290, with tridag.f03).  A CTA owns 32 consecutive
 // lines in i (one per lane) of one plane k, all rows j = 0..ny+1:
-//   phase 1: every warp builds rows j = w, w+W, ... of its lines' systems
-//            (coalesced row loads; off-line neighbours and cross terms
-//            explicit) and stores g = f/m, alpha = a/m, c' (m = b - a c'(j-1))
+//   phase 1: every warp builds the rows of its own segment of the lines'
+//            systems (build_rows: coalesced row loads, a sliding window of
+//            pressure rows; off-line neighbours and cross terms explicit)
+//            and stores g = f'/m, alpha = a/m, c' (m = b - a c'(j-1)), with
+//            the over-relaxation folded in: f' = omega f + (1-omega) T p_old
 //   phase 2: all warps run the two FMA recurrences per line in shared
-//            memory, one row segment each (seg_thomas)
-//   phase 3: every warp writes its rows, relaxed, with the periodic images.
+//            memory, one row segment each (seg_thomas); the solution is the
+//            relaxed line p_old + omega (T^-1 f - p_old)
+//   phase 3: every warp writes its rows with the periodic images.
 // JACOBI: all lines of all planes from the old field pin -> pout.
 // ZEBRA : the lines with one parity of k (launch argument kpar); inside the
 //         CTA the even-i lines first, then the odd-i lines, which see the new
@@ -423,7 +723,8 @@ __device__ __forceinline__ void relax_store(const Geom& g, const T* __restrict__
 //         reference's lexicographic line SOR, Jacobi only across tile edges).
 //         Phase 1 still reads every row once for all 32 lanes: the odd-i
 //         lanes keep f without its six in-plane x-neighbour terms, which are
-//         added after the even-i update (4 coefficient arrays re-read).
+//         added after the even-i update (odd_x_rows: 4 coefficient arrays
+//         and c' re-read).
 //         Own-plane old values come from pin, k+-1 planes from pk (= pin for
 //         the first parity, = pout for the second); output to pout.
 // ZIN: pin is identically zero (first sweep of a correction); zk: pk is too.
@@ -434,123 +735,28 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
                                                     int kpar, int zk, const Blk& B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nj = g.ny + 2, ny = g.ny;
+    const int nj = g.ny + 2;
     T* G = reinterpret_cast<T*>(smem_raw);
     T* AL = G + nj * 32;
     T* CP = AL + nj * 32;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int k = ZEBRA ? 2 * B.x + 1 + kpar : B.x + 1;
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    // x: the 32-line tile (fastest, so the tiles of a plane run together and
+    // read whole rows), y: the plane
+    const int k = ZEBRA ? 2 * B.y + 1 + kpar : B.y + 1;
     if (k > g.nz) return;
-    const int i = B.y * 32 + lane + 1;
+    const int i = B.x * 32 + lane + 1;
     const bool act = i <= g.nx;
     const bool odd = ZEBRA && (i & 1);  // updated in the second half
-    const long long sj = g.sj, sk = g.sk;
-    // old neighbour value at (i+di, j+dj, k+dk)
-    auto P = [&](int j, int di, int dj, int dk) -> T {
-        const long long q = g.at(i + di, j + dj, k + dk);
-        if (dk != 0) return zk ? T(0) : ld(pk, q);
-        return ZIN ? T(0) : ld(pin, q);
-    };
-    const bool noneigh = ZIN && (!ZEBRA || zk);  // every old neighbour is zero
-    if (act) {
-        for (int j = w; j < nj; j += nw) {
-            const long long q = g.at(i, j, k);
-            // a later row of this warp (PLES_LINE_PF_ROWS rows ahead): start
-            // its lines towards L2; the first rows get theirs before the loop
-            if (j == w)
-                for (int d = 1; d < PLES_LINE_PF_ROWS && j + d * nw < nj; ++d) {
-                    const long long qn = q + d * nw * sj;
-                    pf_l2(c.a1, qn); pf_l2(c.b12, qn); pf_l2(c.b13, qn);
-                    pf_l2(c.a2, qn); pf_l2(c.b21, qn); pf_l2(c.b23, qn);
-                    pf_l2(c.a3, qn); pf_l2(c.b31, qn); pf_l2(c.b32, qn);
-                    pf_l2(c.a3, qn - sk); pf_l2(c.b31, qn - sk); pf_l2(c.b32, qn - sk);
-                    pf_l2(rh, qn); pf_l2(cpa, qn);
-                    if (!ZIN) pf_l2(pin, qn + sj);
-                    if (!zk) { pf_l2(pk, qn + sj + sk); pf_l2(pk, qn + sj - sk); }
-                }
-            if (j + PLES_LINE_PF_ROWS * nw < nj) {
-                const long long qn = q + PLES_LINE_PF_ROWS * nw * sj;
-                pf_l2(c.a1, qn); pf_l2(c.b12, qn); pf_l2(c.b13, qn);
-                pf_l2(c.a2, qn); pf_l2(c.b21, qn); pf_l2(c.b23, qn);
-                pf_l2(c.a3, qn); pf_l2(c.b31, qn); pf_l2(c.b32, qn);
-                pf_l2(c.a3, qn - sk); pf_l2(c.b31, qn - sk); pf_l2(c.b32, qn - sk);
-                pf_l2(rh, qn); pf_l2(cpa, qn);
-                if (!ZIN) pf_l2(pin, qn + sj);
-                if (!zk) { pf_l2(pk, qn + sj + sk); pf_l2(pk, qn + sj - sk); }
-            }
-            T f, a, im;
-            if (j == 0) {
-                const T a2 = ld(c.a2, q);
-                f = noneigh ? T(0)
-                            : ld(c.b23, q) * (P(j, 0, 1, 1) + P(j, 0, 0, 1) - P(j, 0, 1, -1) - P(j, 0, 0, -1));
-                if (!odd && !noneigh)
-                    f += ld(c.b21, q) * (P(j, 1, 1, 0) + P(j, 1, 0, 0) - P(j, -1, 1, 0) - P(j, -1, 0, 0));
-                a = T(0);
-                im = T(1) / a2;
-                if (a2 == T(0)) { im = T(1); f = T(0); }  // wall row above a solid cell
-            } else if (j == ny + 1) {
-                const long long qn = q - sj;
-                const T a2 = ld(c.a2, qn);
-                f = noneigh ? T(0)
-                            : -(ld(c.b23, qn) * (P(j, 0, 0, 1) + P(j, 0, -1, 1) - P(j, 0, 0, -1) - P(j, 0, -1, -1)));
-                if (!odd && !noneigh)
-                    f -= ld(c.b21, qn) * (P(j, 1, 0, 0) + P(j, 1, -1, 0) - P(j, -1, 0, 0) - P(j, -1, -1, 0));
-                a = -a2;
-                im = T(1) / (a2 - a * ld(cpa, qn));
-                if (a2 == T(0)) { im = T(1); f = T(0); }  // wall row below a solid cell
-            } else {
-                const T a1e = ld(c.a1, q), a1w = ld(c.a1, q - 1);
-                const T a3f = ld(c.a3, q), a3b = ld(c.a3, q - sk);
-                const T a2 = ld(c.a2, q);
-                a = ld(c.a2, q - sj);
-                const T b = -(a2 + a + a1e + a1w + a3f + a3b);
-                im = T(1) / (b - a * ld(cpa, q - sj));
-                f = ld(rh, q);
-                if (b == T(0)) {  // solid cell of an immersed-boundary mask: identity row
-                    im = T(1);
-                    f = T(0);
-                    a = T(0);
-                }
-                if (!noneigh) {
-                    const T pn = P(j, 0, 1, 0), ps = P(j, 0, -1, 0);
-                    const T pf = P(j, 0, 0, 1), pb = P(j, 0, 0, -1);
-                    const T pef = P(j, 1, 0, 1), peb = P(j, 1, 0, -1), pwf = P(j, -1, 0, 1), pwb = P(j, -1, 0, -1);
-                    const T pnf = P(j, 0, 1, 1), pnb = P(j, 0, 1, -1), psf = P(j, 0, -1, 1), psb = P(j, 0, -1, -1);
-                    const T b12 = ld(c.b12, q), b12w = ld(c.b12, q - 1);
-                    const T b31 = ld(c.b31, q), b31b = ld(c.b31, q - sk);
-                    // every term without an in-plane x-neighbour
-                    T rest = a3f * pf + a3b * pb + (b12 - b12w) * (pn - ps);
-                    rest += ld(c.b13, q) * (pef + pf - peb - pb) - ld(c.b13, q - 1) * (pf + pwf - pb - pwb);
-                    rest += ld(c.b23, q) * (pnf + pf - pnb - pb) - ld(c.b23, q - sj) * (pf + psf - pb - psb);
-                    rest += b31 * (pef - pwf) - b31b * (peb - pwb);
-                    rest += ld(c.b32, q) * (pnf + pn - psf - ps) - ld(c.b32, q - sk) * (pn + pnb - ps - psb);
-                    f -= rest;
-                    if (!odd) {  // the in-plane x-neighbour terms, old values
-                        const T pe = P(j, 1, 0, 0), pw = P(j, -1, 0, 0);
-                        const T pen = P(j, 1, 1, 0), pes = P(j, 1, -1, 0), pwn = P(j, -1, 1, 0), pws = P(j, -1, -1, 0);
-                        const T b21 = ld(c.b21, q), b21s = ld(c.b21, q - sj);
-                        const T tx = a1e * pe + a1w * pw + b12 * (pen - pes) - b12w * (pwn - pws) +
-                                     b21 * (pen + pe - pwn - pw) - b21s * (pe + pes - pw - pws) +
-                                     (b31 - b31b) * (pe - pw);
-                        f -= tx;
-                    }
-                }
-            }
-            G[j * 32 + lane] = f * im;
-            AL[j * 32 + lane] = a * im;
-            // odd lanes keep 1/m here until their x-neighbour terms are added
-            CP[j * 32 + lane] = odd ? im : (j == ny + 1 ? T(0) : ld(cpa, q));
-        }
-    }
+    build_rows<T, ZEBRA, ZIN>(g, c, cpa, pin, pk, rh, omega, zk, i, k, odd, G, AL, CP);
     T* SU = CP + nj * 32;  // segment maps of the parallel Thomas solve
     T* SV = SU + nw * 32;
     const int nhalf = ZEBRA ? 2 : 1;
     for (int half = 0; half < nhalf; ++half) {
         const bool mine = act && (!ZEBRA || ((i & 1) == half));
-        if (ZEBRA && half == 1 && mine) odd_x_terms<T, ZIN>(g, c, cpa, pin, G, CP, i, k);
+        if (ZEBRA && half == 1) odd_x_rows<T, ZIN>(g, c, cpa, pin, omega, G, CP, i, k);
         __syncthreads();
         seg_thomas(G, AL, CP, nj, mine, SU, SV);
-        if (mine) relax_store<T, ZEBRA, ZIN>(g, pin, pout, G, omega, i, k);
+        if (mine) store_rows(g, pout, G, i, k);
         if (ZEBRA) __syncthreads();
     }
 }

@@ -384,7 +384,7 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
         }
         if (staged) {
         } else if (h->smoother != 1) {  // zebra: two launches, k parities
-            dim3 grd((L.g.nz + 1) / 2, (L.g.nx + 31) / 32);
+            dim3 grd((L.g.nx + 31) / 32, (L.g.nz + 1) / 2);
             if (zin) {
                 k_line_relax<T, true, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
                 k_line_relax<T, true, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
@@ -394,7 +394,7 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
             }
             h->launches += 2;
         } else {  // Jacobi over lines
-            dim3 grd(L.g.nz, (L.g.nx + 31) / 32);
+            dim3 grd((L.g.nx + 31) / 32, L.g.nz);
             if (zin)
                 k_line_relax<T, false, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
             else
@@ -687,6 +687,8 @@ int validate(const ples_mg_desc* d, ples_mg_handle* h) {
         return fail(h, PLES_MG_BAD_ARG, "unknown coarsening %d", d->coarsening);
     if (d->jx % 2 || d->jz % 2) return fail(h, PLES_MG_BAD_ARG, "jx and jz must be even");
     if (d->jy > 1000) return fail(h, PLES_MG_BAD_ARG, "jy > 1000 does not fit the line smoother's shared memory");
+    if (make_geom(d->jx, d->jy, d->jz).n >= (1LL << 31))
+        return fail(h, PLES_MG_BAD_ARG, "grid too large: a level box must have fewer than 2^31 elements");
     return PLES_MG_OK;
 }
 
