@@ -51,7 +51,8 @@ typedef struct {
     int jx, jy, jz;        /* fine cells (scala3 jx, jy, jz)                        */
     int ip, jp, kp;        /* 0 periodic, 1 wall (module period, Aboundary.in:6-8);
                               jp must be 1 (multigrid.f03:1744-1746)                */
-    int nlevmax;           /* maximum multigrid levels; 0 = as many as the grid allows */
+    int nlevmax;           /* maximum multigrid levels; 0 = automatic: coarsen until a level has
+                              at most 3072 unknowns (wall rows included), solved by a dense inverse */
     double omega;          /* relaxation factor of the line smoother (0 = default)   */
     int precision;         /* PLES_MG_PREC_*                                        */
     int coords_layout;     /* PLES_MG_COORDS_*                                      */

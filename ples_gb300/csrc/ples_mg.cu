@@ -710,6 +710,85 @@ double mean_spacing(const double* x, const double* y, const double* z, int jx, i
     return n ? s / n : 1.0;
 }
 
+// Gauss-Jordan inversion with partial pivoting on the device (FP64), one
+// pivot column per step over the m x m matrix K and its inverse I:
+//   k_gj_pivot      one CTA: the row p >= col of largest |K(p,col)|; keeps
+//                   K(p,col) and K(col,col) for the step
+//   k_gj_swap_scale thread t: rows p and col swapped in column t, the pivot
+//                   row scaled by 1/K(p,col); the elimination factors
+//                   f(r) = K(r,col) after the swap (0 for the pivot row)
+//   k_gj_eliminate  K(r,q) -= f(r) K(col,q) (q >= col; the columns before
+//                   are unit columns already) and I(r,q) -= f(r) I(col,q)
+struct GjStep {
+    int piv;
+    int bad;
+    double pv, kcc;
+};
+__global__ void k_gj_pivot(const double* __restrict__ K, int m, int col, GjStep* st) {
+    __shared__ double bv[1024];
+    __shared__ int bi[1024];
+    double best = -1.0;
+    int arg = col;
+    for (int r = col + (int)threadIdx.x; r < m; r += blockDim.x) {
+        const double v = fabs(K[(size_t)r * m + col]);
+        if (v > best) { best = v; arg = r; }
+    }
+    bv[threadIdx.x] = best;
+    bi[threadIdx.x] = arg;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            const double v = bv[threadIdx.x + o];
+            const int a = bi[threadIdx.x + o];
+            if (v > bv[threadIdx.x] || (v == bv[threadIdx.x] && a < bi[threadIdx.x])) {
+                bv[threadIdx.x] = v;
+                bi[threadIdx.x] = a;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int p = bi[0];
+        st->piv = p;
+        if (!(bv[0] > 0.0)) st->bad = 1;
+        st->pv = K[(size_t)p * m + col];
+        st->kcc = K[(size_t)col * m + col];
+    }
+}
+__global__ void k_gj_swap_scale(double* __restrict__ K, double* __restrict__ I, double* __restrict__ f, int m,
+                                int col, const GjStep* st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m || st->bad) return;
+    const int p = st->piv;
+    const double inv = 1.0 / st->pv;
+    // factor of row t after the swap (rows other than p and col keep theirs)
+    f[t] = t == col ? 0.0 : (t == p ? st->kcc : K[(size_t)t * m + col]);
+    const double ka = K[(size_t)p * m + t], kb = K[(size_t)col * m + t];
+    const double ia = I[(size_t)p * m + t], ib = I[(size_t)col * m + t];
+    if (p != col) {
+        K[(size_t)p * m + t] = kb;
+        I[(size_t)p * m + t] = ib;
+    }
+    K[(size_t)col * m + t] = ka * inv;
+    I[(size_t)col * m + t] = ia * inv;
+}
+__global__ void k_gj_eliminate(double* __restrict__ K, double* __restrict__ I, const double* __restrict__ f, int m,
+                               int col, const GjStep* st) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    if (q >= m || r == col || st->bad) return;
+    const double fr = f[r];
+    if (fr == 0.0) return;
+    if (q >= col) K[(size_t)r * m + q] -= fr * K[(size_t)col * m + q];
+    I[(size_t)r * m + q] -= fr * I[(size_t)col * m + q];
+}
+template <typename T>
+__global__ void k_gj_extract(const double* __restrict__ I, int m, int n, T* __restrict__ S) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    if (q < n) S[(size_t)r * n + q] = T(I[(size_t)r * m + q]);
+}
+
 // dense inverse of the bordered coarsest system [[M, v], [1^T, 0]] (M: the
 // level operator on interior cells and wall ghost rows, periodic in x/z;
 // v: its left null vector, +1 on interior rows and -1 on wall rows)
@@ -802,41 +881,51 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
             K[(size_t)n * m + u] = 1.0;
         }
     }
-    // Gauss-Jordan inverse with partial pivoting
+    // Gauss-Jordan inverse with partial pivoting, on the device
     std::vector<double> I((size_t)m * m, 0.0);
     for (int u = 0; u < m; ++u) I[(size_t)u * m + u] = 1.0;
-    for (int col = 0; col < m; ++col) {
-        int piv = col;
-        double best = std::fabs(K[(size_t)col * m + col]);
-        for (int r = col + 1; r < m; ++r) {
-            double v = std::fabs(K[(size_t)r * m + col]);
-            if (v > best) { best = v; piv = r; }
+    std::vector<void*> tmp;
+    auto talloc = [&](void** p, size_t bytes) -> int {
+        if (cudaMalloc(p, bytes) != cudaSuccess) {
+            *p = nullptr;
+            free_tmp(tmp);
+            return fail(h, PLES_MG_OOM, "cudaMalloc(%zu) failed for the coarsest-level inverse", bytes);
         }
-        if (!(best > 0.0)) return fail(h, PLES_MG_BAD_ARG, "coarsest-level system is singular");
-        if (piv != col)
-            for (int q = 0; q < m; ++q) {
-                std::swap(K[(size_t)piv * m + q], K[(size_t)col * m + q]);
-                std::swap(I[(size_t)piv * m + q], I[(size_t)col * m + q]);
-            }
-        const double inv = 1.0 / K[(size_t)col * m + col];
-        for (int q = 0; q < m; ++q) { K[(size_t)col * m + q] *= inv; I[(size_t)col * m + q] *= inv; }
-        for (int r = 0; r < m; ++r) {
-            if (r == col) continue;
-            const double f = K[(size_t)r * m + col];
-            if (f == 0.0) continue;
-            for (int q = 0; q < m; ++q) {
-                K[(size_t)r * m + q] -= f * K[(size_t)col * m + q];
-                I[(size_t)r * m + q] -= f * I[(size_t)col * m + q];
-            }
+        tmp.push_back(*p);
+        return PLES_MG_OK;
+    };
+    double *dK, *dI, *dF;
+    GjStep* dS;
+    int rc;
+    if ((rc = talloc((void**)&dK, 8 * (size_t)m * m)) || (rc = talloc((void**)&dI, 8 * (size_t)m * m)) ||
+        (rc = talloc((void**)&dF, 8 * (size_t)m)) || (rc = talloc((void**)&dS, sizeof(GjStep))))
+        return rc;
+    auto gj = [&]() -> int {
+        CK(cudaMemcpyAsync(dK, K.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(dI, I.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemsetAsync(dS, 0, sizeof(GjStep), h->st));
+        const int tb = 256, nb = (m + tb - 1) / tb;
+        for (int col = 0; col < m; ++col) {
+            k_gj_pivot<<<1, 1024, 0, h->st>>>(dK, m, col, dS);
+            k_gj_swap_scale<<<nb, tb, 0, h->st>>>(dK, dI, dF, m, col, dS);
+            k_gj_eliminate<<<dim3(nb, m), tb, 0, h->st>>>(dK, dI, dF, m, col, dS);
         }
-    }
-    std::vector<T> S((size_t)n * n);
-    for (int r = 0; r < n; ++r)
-        for (int q = 0; q < n; ++q) S[(size_t)r * n + q] = T(I[(size_t)r * m + q]);
-    int rc = dalloc(h, &h->coarse_S, sizeof(T) * (size_t)n * n);
+        h->launches += 3LL * m;
+        CK(cudaGetLastError());
+        GjStep hs;
+        CK(cudaMemcpyAsync(&hs, dS, sizeof(GjStep), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        if (hs.bad) return fail(h, PLES_MG_BAD_ARG, "coarsest-level system is singular");
+        if ((rc = dalloc(h, &h->coarse_S, sizeof(T) * (size_t)n * n))) return rc;
+        k_gj_extract<T><<<dim3((n + 255) / 256, n), 256, 0, h->st>>>(dI, m, n, (T*)h->coarse_S);
+        ++h->launches;
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(h->st));
+        return PLES_MG_OK;
+    };
+    rc = gj();
+    free_tmp(tmp);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(h->coarse_S, S.data(), sizeof(T) * (size_t)n * n, cudaMemcpyHostToDevice, h->st));
-    CK(cudaStreamSynchronize(h->st));
     h->coarse_n = n;
     return PLES_MG_OK;
 }
@@ -900,7 +989,9 @@ void mask_coef(ples_mg_handle* h, int lev, Coef<T>& c) {
     ++h->launches;
 }
 
-constexpr int kDenseMax = 640;  // largest coarsest system solved by the dense inverse
+// largest coarsest system solved by the dense inverse (unknowns, wall rows
+// included): coarsening stops at the first level at or below it
+constexpr int kDenseMax = 3072;
 
 int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     int rc = validate(d, h);
@@ -951,6 +1042,8 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         const bool can_x = nx % 2 == 0 && nx / 2 >= 2;
         const bool can_z = nz % 2 == 0 && nz / 2 >= 2;
         if (!can_y) break;
+        // automatic depth: the dense coarsest solve from the first level small enough
+        if (d->nlevmax == 0 && nl >= 2 && (long long)nx * nz * (ny + 2) <= kDenseMax) break;
         int rx, rz;
         if (d->coarsening == 0) {
             if (!can_x || !can_z) break;

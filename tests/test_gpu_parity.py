@@ -46,8 +46,8 @@ def case0():
 
 @pytest.fixture(scope="module")
 def dev_full(case0):
-    """The reference's full-coarsening hierarchy (mul_met levels)."""
-    with mg.Multigrid(case0["x"], case0["y"], case0["z"], precision="mixed") as m:
+    """The reference's full-coarsening hierarchy (mul_met levels, four of them)."""
+    with mg.Multigrid(case0["x"], case0["y"], case0["z"], precision="mixed", nlevmax=4) as m:
         yield m
 
 
@@ -84,7 +84,7 @@ def test_metric_sample_deck_and_ghosted_layout():
     orc = Oracle(x, y, z)
     # the ghosted (-8:n+8) layout as PLES holds it after cellep
     gx, gy, gz = (orc.coords(c) for c in range(3))
-    with mg.Multigrid(gx, gy, gz, coords_layout=mg.COORDS_GHOSTED8) as m:
+    with mg.Multigrid(gx, gy, gz, coords_layout=mg.COORDS_GHOSTED8, nlevmax=4) as m:
         assert (m.jx, m.jy, m.jz) == (32, 32, 32)
         for level in (1, 2, 3, 4):
             for name in mg.METRIC_NAMES:
