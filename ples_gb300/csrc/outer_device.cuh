@@ -94,6 +94,38 @@ __device__ __forceinline__ void k_resid_outer2_blk(Geom g, Coef<double> c, const
         pmax[blk] = m;
     }
 }
+// the same residual when x is zero everywhere in the box: r = b exactly
+// (every flux vanishes), written and reduced with the same block layout
+template <typename Ti, int KC>
+__device__ __forceinline__ void k_resid_zero_blk(Geom g, const double* __restrict__ b, Ti* __restrict__ rin,
+                                                 double* __restrict__ psq, double* __restrict__ pmax, const Blk& B) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = B.x * 32 + tx + 1, j = B.y * 8 + ty + 1;
+    const int k0 = B.z * KC + 1, k1 = min(k0 + KC - 1, g.nz);
+    double s = 0.0, m = 0.0;
+    if (i <= g.nx && j <= g.ny)
+        for (int k = k0; k <= k1; ++k) {
+            const long long q = g.at(i, j, k);
+            const double r = b[q];
+            rin[q] = Ti(r);
+            s += r * r;
+            m = fmax(m, fabs(r));
+        }
+    block_reduce_sum_max(s, m);
+    if (threadIdx.x == 0) {
+        const long long blk = ((long long)B.z * B.gy + B.y) * B.gx + B.x;
+        psq[blk] = s;
+        pmax[blk] = m;
+    }
+}
+// flag := 1 if any element of the box is nonzero (flag cleared before)
+__device__ __forceinline__ void k_box_nonzero_blk(long long n, const double* __restrict__ x, int* __restrict__ flag,
+                                                  const Blk& B) {
+    bool nz = false;
+    for (long long q = (long long)B.x * blockDim.x + threadIdx.x; q < n; q += (long long)B.gx * blockDim.x)
+        nz |= x[q] != 0.0;
+    if (__syncthreads_or(nz) && threadIdx.x == 0) *flag = 1;
+}
 // sum / sum of squares of interior cells, per-block partials
 __device__ __forceinline__ void k_sum_interior_blk(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum, const Blk& B) {
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;

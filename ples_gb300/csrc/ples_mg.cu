@@ -59,6 +59,22 @@ __global__ void __launch_bounds__(256) k_resid_outer2(Geom g, Coef<double> c, co
     k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk());
 }
 
+// the first residual of a solve: the stencil is skipped when the initial
+// guess (wall ghosts included) is zero everywhere, *xnz == 0
+template <typename Ti, int KC>
+__global__ void __launch_bounds__(256) k_resid_outer2_first(Geom g, Coef<double> c, const double* __restrict__ x,
+                                                            const double* __restrict__ b, Ti* __restrict__ rin,
+                                                            double* __restrict__ psq, double* __restrict__ pmax,
+                                                            const int* __restrict__ xnz) {
+    if (*xnz == 0)
+        k_resid_zero_blk<Ti, KC>(g, b, rin, psq, pmax, hw_blk());
+    else
+        k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk());
+}
+__global__ void k_box_nonzero(long long n, const double* __restrict__ x, int* __restrict__ flag) {
+    k_box_nonzero_blk(n, x, flag, hw_blk());
+}
+
 __global__ void k_sum_interior(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum) {
     k_sum_interior_blk(g, a, squares, psum, hw_blk());
 }
@@ -556,10 +572,19 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     // the device work between two stop tests: the FP64 residual of x (after
     // its wall fill) with its norms copied to h_red, preceded from the second
     // test on by the V-cycles and the update
-    auto enqueue_residual = [&]() {
+    auto enqueue_residual = [&](bool first) {
         wall_fill(h, h->x, h->cs_c[2], h->cs_c[3], 1.0 / dt, h->wall_passes, g, F.cd);
         timed_begin(h, KIND_OUTER, 1);
-        k_resid_outer2<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b);
+        if (first) {  // a zero initial guess needs no stencil
+            int* xnz = reinterpret_cast<int*>(h->red + 5);
+            cudaMemsetAsync(xnz, 0, sizeof(int), h->st);
+            k_box_nonzero<<<1216, 256, 0, h->st>>>(g.n, h->x, xnz);  // 8 CTAs per SM of a GB300
+            k_resid_outer2_first<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b,
+                                                               xnz);
+            ++h->launches;
+        } else {
+            k_resid_outer2<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b);
+        }
         timed_end(h, KIND_OUTER, 1);
         k_reduce_final<<<1, 1024, 0, h->st>>>(h->part_a, h->part_b, nblk, h->red);
         h->launches += 2;
@@ -569,7 +594,7 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         for (int c = 0; c < h->inner_cycles; ++c) vcycle<T>(h, c == 0);
         k_update<T><<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, (const T*)F.p);
         ++h->launches;
-        enqueue_residual();
+        enqueue_residual(false);
     };
     // graph replays of enqueue_iteration (the timing events, if any, are
     // nodes of the graph)
@@ -613,7 +638,7 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     }
     double rel = 0.0, rmax = 0.0, rel0 = -1.0;
     int it = 0, status = PLES_MG_NOT_CONVERGED, vcyc = 0;
-    enqueue_residual();
+    enqueue_residual(true);
     CK(cudaGetLastError());
     for (;;) {
         CK(cudaStreamSynchronize(h->st));
