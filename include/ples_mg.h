@@ -191,9 +191,9 @@ int ples_mg_step(ples_mg_handle *h, double *u, double *v, double *w, double *uc,
 /* ---- autotuner ----------------------------------------------------------
  * No counterpart in the reference (its kss, nlevel and omega are fixed
  * inputs).  Times candidate settings on this handle's grid and keeps the
- * fastest: the CTA width of the eta-line smoother per level (128 or 256
+ * fastest: the CTA width of the eta-line smoother per level (128, 256 or 512
  * threads, by kernel time) and then the sweeps per level (nu_pre = nu_post
- * in 1..3) and V-cycles per outer iteration (2, 3, 4, 6), by the time of a
+ * in 1..3) and V-cycles per outer iteration (2 to 6), by the time of a
  * whole solve to ||r||/||b|| <= 1e-10 from zero.  rhs (host, (1:jx,1:jy,
  * 1:jz)) or NULL for a pseudo-random compatible one.  Batches created
  * afterwards use the tuned settings of their members. */

@@ -420,7 +420,7 @@ int build_steps(ples_mg_batch* b) {
                 const long long cells = (long long)L.g.nx * L.g.ny * L.g.nz;
                 if (cells > big) {
                     big = cells;
-                    B.cur.threads = L.line_threads;
+                    B.cur.threads = std::min(L.line_threads, 256);  // kb_line is built for 256
                 }
             }
             B.end();

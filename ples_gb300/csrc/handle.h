@@ -31,7 +31,7 @@ struct LevelData {
     bool has_cf = false, has_cd = false;
     // TMA-staged zebra smoother (FP32): tensor maps of this level's fields;
     // pA/pB are the buffers behind maps.pA/pB (p and p2 swap every sweep)
-    int line_threads = 256;  // CTA width of the eta-line smoother (128 or 256; autotuned)
+    int line_threads = 256;  // CTA width of the eta-line smoother (128, 256 or 512; autotuned)
     bool tma = false;
     void *pA = nullptr, *pB = nullptr;
     ples::LineMaps maps{};

@@ -728,7 +728,7 @@ __device__ __forceinline__ void relax_store(const Geom& g, const T* __restrict__
 //         Own-plane old values come from pin, k+-1 planes from pk (= pin for
 //         the first parity, = pout for the second); output to pout.
 // ZIN: pin is identically zero (first sweep of a correction); zk: pk is too.
-// Shared memory: 3 arrays [ny+2][32] and the segment maps [2][8][32].
+// Shared memory: 3 arrays [ny+2][32] and the segment maps [2][warps][32].
 template <typename T, bool ZEBRA, bool ZIN>
 __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
@@ -759,6 +759,15 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
         if (mine) store_rows(g, pout, G, i, k);
         if (ZEBRA) __syncthreads();
     }
+}
+// the same smoother with 16 warps per CTA (shorter row segments per warp,
+// for coarse levels whose few CTAs leave most SMs idle)
+template <typename T, bool ZEBRA, bool ZIN>
+__global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) k_line_relax_w(Geom g, Coef<T> c, const T* __restrict__ cpa,
+                                                    const T* __restrict__ pin, const T* __restrict__ pk,
+                                                    T* __restrict__ pout, const T* __restrict__ rh, T omega,
+                                                    int kpar, int zk) {
+    k_line_relax_blk<T, ZEBRA, ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
 }
 template <typename T, bool ZEBRA, bool ZIN>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? PLES_LINE_MIN_BLOCKS : 2) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,

@@ -277,8 +277,11 @@ void ghost_xz(ples_mg_handle* h, const Geom& g, T* p) {
     ++h->launches;
 }
 
+// G, alpha, c' rows and the segment maps of one CTA of the line smoother
 template <typename T>
-size_t line_smem(const Geom& g) { return (3 * (size_t)(g.ny + 2) + 2 * 8) * 32 * sizeof(T); }
+size_t line_smem(const Geom& g, int threads = 256) {
+    return (3 * (size_t)(g.ny + 2) + 2 * (size_t)(threads / 32)) * 32 * sizeof(T);
+}
 
 // the dynamic shared-memory limit is a per-function attribute shared by all
 // handles of the process: only ever raise it
@@ -291,6 +294,8 @@ int set_smem_attrs(ples_mg_handle* h, size_t smem) {
     CK(cudaFuncSetAttribute(k_line_relax<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_w<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_w<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_dense_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
 }
@@ -370,7 +375,8 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
     if (zero && nu == 0) cudaMemsetAsync(L.p, 0, sizeof(T) * (size_t)L.g.n, h->st);
     const Coef<T> c = coef_of<T>(L);
     const T om = T(h->omega);
-    const size_t smem = line_smem<T>(L.g);
+    const int nt = h->smoother == 1 ? std::min(L.line_threads, 256) : L.line_threads;
+    const size_t smem = line_smem<T>(L.g, nt);
     const T* cp = (const T*)L.cp;
     for (int s = 0; s < nu; ++s) {
         const bool zin = zero && s == 0;
@@ -401,20 +407,17 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
         if (staged) {
         } else if (h->smoother != 1) {  // zebra: two launches, k parities
             dim3 grd((L.g.nx + 31) / 32, (L.g.nz + 1) / 2);
-            if (zin) {
-                k_line_relax<T, true, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
-                k_line_relax<T, true, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
-            } else {
-                k_line_relax<T, true, false><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
-                k_line_relax<T, true, false><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
-            }
+            auto kern = nt > 256 ? (zin ? k_line_relax_w<T, true, true> : k_line_relax_w<T, true, false>)
+                                 : (zin ? k_line_relax<T, true, true> : k_line_relax<T, true, false>);
+            kern<<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
+            kern<<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
             h->launches += 2;
         } else {  // Jacobi over lines
             dim3 grd((L.g.nx + 31) / 32, L.g.nz);
             if (zin)
-                k_line_relax<T, false, true><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
+                k_line_relax<T, false, true><<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
             else
-                k_line_relax<T, false, false><<<grd, L.line_threads, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
+                k_line_relax<T, false, false><<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
             ++h->launches;
         }
         timed_end(h, KIND_LINE, level);
@@ -1134,7 +1137,17 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
             k_line_lu<double><<<lg, 128, 0, h->st>>>(L.g, L.cd, (double*)L.cp);
         CK(cudaGetLastError());
         size_t sm = mixed ? line_smem<float>(L.g) : line_smem<double>(L.g);
-        smem_max = std::max(smem_max, sm);
+        if (sm > 227 * 1024) return fail(h, PLES_MG_BAD_ARG, "eta lines too long for shared memory");
+        // a level whose zebra launch has fewer CTAs than two per SM gets the
+        // 16-warp form: its time is each CTA's chain of row steps
+        {
+            const long long ctas = (long long)((L.g.nx + 31) / 32) * ((L.g.nz + 1) / 2);
+            const size_t sw = mixed ? line_smem<float>(L.g, 512) : line_smem<double>(L.g, 512);
+            L.line_threads = ctas < 2 * 152 && sw <= 227 * 1024 ? 512 : 256;
+        }
+        // room for the 16-warp form where it fits
+        sm = std::max(sm, mixed ? line_smem<float>(L.g, 512) : line_smem<double>(L.g, 512));
+        smem_max = std::max(smem_max, std::min(sm, (size_t)227 * 1024));
         if (mixed && h->smoother == 2 && line_tma_smem(L.g.ny) <= 227 * 1024) {
             if ((rc = build_line_maps(h, L)) || (rc = set_tma_smem_attr(h, line_tma_smem(L.g.ny)))) return rc;
         }
@@ -1881,7 +1894,11 @@ int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) 
         for (int n = 0; n < nsmooth; ++n) {
             double best = 1e300;
             int bt = h->L[n].line_threads;
-            for (int t : {128, 256}) {
+            for (int t : {128, 256, 512}) {
+                const LevelData& Ln = h->L[n];
+                const size_t need = h->d.precision == PLES_MG_PREC_MIXED ? line_smem<float>(Ln.g, t)
+                                                                          : line_smem<double>(Ln.g, t);
+                if (need > 227 * 1024) continue;
                 h->L[n].line_threads = t;
                 ples_mg_kernel_timing(h, KIND_LINE, n + 1);
                 if ((rc = trial(1, &ms, &st))) return rc;
@@ -1900,7 +1917,7 @@ int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) 
         int bnu = h->nu_pre, bin = h->inner_cycles;
         double bms = 1e300;
         for (int nu : {1, 2, 3})
-            for (int inner : {2, 3, 4, 6}) {
+            for (int inner : {2, 3, 4, 5, 6}) {
                 h->nu_pre = h->nu_post = nu;
                 h->inner_cycles = inner;
                 if ((rc = trial(1, &ms, &st)) || (rc = trial(2, &ms, &st))) return rc;
