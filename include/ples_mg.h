@@ -188,6 +188,17 @@ int ples_mg_project(ples_mg_handle *h, double *uc, double *vc, double *wc, doubl
 int ples_mg_step(ples_mg_handle *h, double *u, double *v, double *w, double *uc, double *vc,
                  double *wc, double *fi, double rel_tol, int max_cycles, ples_mg_stats *stats);
 
+/* ---- grid file ------------------------------------------------------------
+ * Reads PLES's grid file gri3dp_in.dat as fsrc/stratiParticle.f03:364-412
+ * does (list-directed: the lengths alx aly alz, the cell counts jx jy jz,
+ * then one record per coordinate, x y z of every node, i fastest).  With
+ * x, y, z all NULL only lengths (may be NULL) and dims are filled; then call
+ * again with three caller arrays of (jx+1)(jy+1)(jz+1) doubles, which take
+ * the node coordinates in the (0:jx,0:jy,0:jz) layout of ples_mg_desc.
+ * Needs no device.  BAD_ARG for a missing or malformed file. */
+int ples_mg_read_grid(const char *path, double lengths[3], int dims[3], double *x, double *y,
+                      double *z);
+
 /* ---- autotuner ----------------------------------------------------------
  * No counterpart in the reference (its kss, nlevel and omega are fixed
  * inputs).  Times candidate settings on this handle's grid and keeps the

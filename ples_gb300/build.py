@@ -1,11 +1,12 @@
 """Build the CUDA library libples_mg.so in-tree for GB300 (sm_103a).
 
-Three translation units compiled in parallel with nvcc and linked into one
+Four translation units compiled in parallel with nvcc and linked into one
 shared object under ples_gb300/_build/:
   csrc/metric.cu   -- device face metric, compiled with -fmad=false so its
                       FP64 arithmetic is rounded as written
   csrc/ples_mg.cu  -- stencil kernels, V-cycle driver and the C ABI
   csrc/batch.cu    -- batched solves of many grids and the request server
+  csrc/grid_io.cpp -- reader of PLES's grid file (host code)
 The library depends on the CUDA runtime only (statically linked); PyTorch is
 not needed to build or load it.
 """
@@ -52,10 +53,10 @@ def build(force=False, verbose=False, extra=()):
     nvcc = nvcc_path()
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", SRC,
               "-I", os.path.join(ROOT, "include")] + ARCH + list(extra)
-    units = [("metric.cu", ["-fmad=false"]), ("ples_mg.cu", []), ("batch.cu", [])]
+    units = [("metric.cu", ["-fmad=false"]), ("ples_mg.cu", []), ("batch.cu", []), ("grid_io.cpp", [])]
     procs = []
     for name, flags in units:
-        obj = os.path.join(OUT, name.replace(".cu", ".o"))
+        obj = os.path.join(OUT, os.path.splitext(name)[0] + ".o")
         cmd = [nvcc] + common + flags + ["-c", os.path.join(SRC, name), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)

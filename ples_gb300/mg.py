@@ -70,7 +70,7 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_batch_solve", "ples_mg_batch_solve_device", "ples_mg_batch_info",
            "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
            "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune", "ples_mg_project",
-           "ples_mg_step", "ples_mg_residual_norms_device")
+           "ples_mg_step", "ples_mg_residual_norms_device", "ples_mg_read_grid")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -108,6 +108,7 @@ def load(build=True):
     L.ples_mg_autotune.argtypes = [vp, vp, C.POINTER(Tuning)]
     L.ples_mg_project.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_step.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
+    L.ples_mg_read_grid.argtypes = [C.c_char_p, vp, vp, vp, vp, vp]
     L.ples_mg_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
     L.ples_mg_batch_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
     L.ples_mg_batch_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
@@ -137,6 +138,23 @@ def _cs_ptrs(cs):
     keep = [None if a is None else _f64(a) for a in cs]
     arr = (C.c_void_p * 6)(*[None if a is None else a.ctypes.data for a in keep])
     return C.cast(arr, C.c_void_p), (keep, arr)
+
+
+def read_grid(path):
+    """PLES's grid file through ples_mg_read_grid: returns (lengths, (jx, jy,
+    jz), (x, y, z)) with node arrays (jx+1, jy+1, jz+1) in Fortran order."""
+    L = load()
+    lengths = (C.c_double * 3)()
+    dims = (C.c_int * 3)()
+    rc = L.ples_mg_read_grid(os.fsencode(path), lengths, dims, None, None, None)
+    if rc:
+        raise PlesMGError(rc, f"{L.ples_mg_strerror(rc).decode()}: cannot read grid file {path}")
+    jx, jy, jz = dims
+    xyz = [np.zeros((jx + 1, jy + 1, jz + 1), order="F") for _ in range(3)]
+    rc = L.ples_mg_read_grid(os.fsencode(path), lengths, dims, *[C.c_void_p(a.ctypes.data) for a in xyz])
+    if rc:
+        raise PlesMGError(rc, f"{L.ples_mg_strerror(rc).decode()}: malformed grid file {path}")
+    return tuple(lengths), (jx, jy, jz), tuple(xyz)
 
 
 class Multigrid:
