@@ -39,6 +39,7 @@ module ples_mg_iface
         integer(c_int) :: smoother
         integer(c_int) :: coarsening
         type(c_ptr)    :: solid
+        type(c_ptr)    :: tipo
     end type ples_mg_desc
 
     type, bind(C) :: ples_mg_stats
@@ -99,7 +100,7 @@ contains
                          precision=precision, coords_layout=PLES_MG_COORDS_GHOSTED8, &
                          x=c_loc(x(-8, -8, -8)), y=c_loc(y(-8, -8, -8)), z=c_loc(z(-8, -8, -8)), &
                          dt=dt, device=0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0, &
-                         smoother=0, coarsening=0, solid=c_null_ptr)
+                         smoother=0, coarsening=0, solid=c_null_ptr, tipo=c_null_ptr)
         if (c_associated(mg_handle)) call ples_mg_destroy(mg_handle)
         stat = ples_mg_create(d, mg_handle)
         if (stat /= PLES_MG_OK) error stop 'ples_mg_create failed'

@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define PLES_MG_ABI_VERSION 2
+#define PLES_MG_ABI_VERSION 3
 
 /* status codes */
 enum {
@@ -73,6 +73,13 @@ typedef struct {
                               from the system (Neumann at their faces); the
                               solution is 0 there and rhs, compatibility and
                               mean refer to the fluid cells.  Not for batches. */
+    const int *tipo;       /* PLES's immersed-boundary cell types (0:jx+1,0:jy+1,
+                              0:jz+1) (0 solid, 1 IB, >= 2 fluid), or NULL.  As
+                              in multi with bodyforce = 1 (multigrid.f03:615-
+                              631), the max-norm stop test (eps / max_residual)
+                              then runs over the fluid cells only; the operator
+                              is unchanged.  Also the input of
+                              ples_mg_potenziale_ibm.  Not for batches. */
 } ples_mg_desc;
 
 typedef struct {
@@ -187,6 +194,13 @@ int ples_mg_project(ples_mg_handle *h, double *uc, double *vc, double *wc, doubl
  * (fsrc/stratiParticle.f03:2845-2937). */
 int ples_mg_step(ples_mg_handle *h, double *u, double *v, double *w, double *uc, double *vc,
                  double *wc, double *fi, double rel_tol, int max_cycles, ples_mg_stats *stats);
+
+/* potenziale_ibm (fsrc/potenziale_ibm.f03:37-88): every solid cell (tipo 0)
+ * of fi takes the mean of its face neighbours that are IB cells (tipo 1), in
+ * the order i+1, i-1, j+1, j-1, k+1, k-1, and keeps its value if it has
+ * none.  fi (0:jx+1,0:jy+1,0:jz+1) host, in/out; ghost cells are read, not
+ * written.  Needs the descriptor's tipo (BAD_ARG without). */
+int ples_mg_potenziale_ibm(ples_mg_handle *h, double *fi);
 
 /* ---- grid file ------------------------------------------------------------
  * Reads PLES's grid file gri3dp_in.dat as fsrc/stratiParticle.f03:364-412

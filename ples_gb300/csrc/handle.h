@@ -52,6 +52,7 @@ struct ples_mg_handle {
     int* dflag = nullptr;                                // bounded-wait error flag, inside red
     double* h_red = nullptr;                             // pinned host copy
     double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
+    uint8_t* tipo = nullptr;  // level-1 cell types (0 solid, 1 IB, 2 fluid, 3 other), or null
     double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes
     double* cs_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // their device buffers
     // projection step (diver / gradie / vel_up), allocated on first use:

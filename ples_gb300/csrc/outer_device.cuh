@@ -59,7 +59,8 @@ __device__ __forceinline__ double flux_z(const Geom& g, const Coef<double>& c, c
 template <typename Ti, int KC>
 __device__ __forceinline__ void k_resid_outer2_blk(Geom g, Coef<double> c, const double* __restrict__ x,
                                                       const double* __restrict__ b, Ti* __restrict__ rin,
-                                                      double* __restrict__ psq, double* __restrict__ pmax, const Blk& B) {
+                                                      double* __restrict__ psq, double* __restrict__ pmax, const Blk& B,
+                                                      const uint8_t* __restrict__ tipo = nullptr) {
     __shared__ double sN[8][32];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i = B.x * 32 + tx + 1, j = B.y * 8 + ty + 1;
@@ -83,7 +84,7 @@ __device__ __forceinline__ void k_resid_outer2_blk(Geom g, Coef<double> c, const
             const double r = b[q] - ((fE - fW) + (fN - fS) + (fF - fB));
             rin[q] = Ti(r);
             s += r * r;
-            m = fmax(m, fabs(r));
+            if (!tipo || tipo[q] == 2) m = fmax(m, fabs(r));  // max over fluid cells (tipo >= 2)
         }
         fB = fF;
     }
@@ -98,7 +99,8 @@ __device__ __forceinline__ void k_resid_outer2_blk(Geom g, Coef<double> c, const
 // (every flux vanishes), written and reduced with the same block layout
 template <typename Ti, int KC>
 __device__ __forceinline__ void k_resid_zero_blk(Geom g, const double* __restrict__ b, Ti* __restrict__ rin,
-                                                 double* __restrict__ psq, double* __restrict__ pmax, const Blk& B) {
+                                                 double* __restrict__ psq, double* __restrict__ pmax, const Blk& B,
+                                                 const uint8_t* __restrict__ tipo = nullptr) {
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i = B.x * 32 + tx + 1, j = B.y * 8 + ty + 1;
     const int k0 = B.z * KC + 1, k1 = min(k0 + KC - 1, g.nz);
@@ -109,7 +111,7 @@ __device__ __forceinline__ void k_resid_zero_blk(Geom g, const double* __restric
             const double r = b[q];
             rin[q] = Ti(r);
             s += r * r;
-            m = fmax(m, fabs(r));
+            if (!tipo || tipo[q] == 2) m = fmax(m, fabs(r));
         }
     block_reduce_sum_max(s, m);
     if (threadIdx.x == 0) {
@@ -125,6 +127,29 @@ __device__ __forceinline__ void k_box_nonzero_blk(long long n, const double* __r
     for (long long q = (long long)B.x * blockDim.x + threadIdx.x; q < n; q += (long long)B.gx * blockDim.x)
         nz |= x[q] != 0.0;
     if (__syncthreads_or(nz) && threadIdx.x == 0) *flag = 1;
+}
+// potenziale_ibm (potenziale_ibm.f03:37-88): a solid cell (tipo 0) takes
+// the mean of its IB face neighbours (tipo 1), summed from zero in the order
+// i+1, i-1, j+1, j-1, k+1, k-1; with none it keeps its value.  Only solid
+// cells are written and only IB cells are read, so cells are independent.
+__device__ __forceinline__ void k_potenziale_ibm_blk(Geom g, const uint8_t* __restrict__ tipo, double* __restrict__ fi,
+                                                     const Blk& B) {
+    const int i = B.x * blockDim.x + threadIdx.x + 1;
+    const int j = B.y * blockDim.y + threadIdx.y + 1;
+    const int k = B.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const long long q = g.at(i, j, k);
+    if (tipo[q] != 0) return;
+    const long long nb[6] = {q + 1, q - 1, q + g.sj, q - g.sj, q + g.sk, q - g.sk};
+    double s = 0.0;
+    int cnt = 0;
+#pragma unroll
+    for (int d = 0; d < 6; ++d)
+        if (tipo[nb[d]] == 1) {
+            s = s + fi[nb[d]];
+            ++cnt;
+        }
+    if (cnt) fi[q] = s / cnt;
 }
 // sum / sum of squares of interior cells, per-block partials
 __device__ __forceinline__ void k_sum_interior_blk(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum, const Blk& B) {

@@ -55,8 +55,9 @@ __global__ void k_scale_coef(long long n, const double* __restrict__ g11, const 
 template <typename Ti, int KC>
 __global__ void __launch_bounds__(256) k_resid_outer2(Geom g, Coef<double> c, const double* __restrict__ x,
                                                       const double* __restrict__ b, Ti* __restrict__ rin,
-                                                      double* __restrict__ psq, double* __restrict__ pmax) {
-    k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk());
+                                                      double* __restrict__ psq, double* __restrict__ pmax,
+                                                      const uint8_t* __restrict__ tipo) {
+    k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk(), tipo);
 }
 
 // the first residual of a solve: the stencil is skipped when the initial
@@ -65,11 +66,15 @@ template <typename Ti, int KC>
 __global__ void __launch_bounds__(256) k_resid_outer2_first(Geom g, Coef<double> c, const double* __restrict__ x,
                                                             const double* __restrict__ b, Ti* __restrict__ rin,
                                                             double* __restrict__ psq, double* __restrict__ pmax,
-                                                            const int* __restrict__ xnz) {
+                                                            const int* __restrict__ xnz,
+                                                            const uint8_t* __restrict__ tipo) {
     if (*xnz == 0)
-        k_resid_zero_blk<Ti, KC>(g, b, rin, psq, pmax, hw_blk());
+        k_resid_zero_blk<Ti, KC>(g, b, rin, psq, pmax, hw_blk(), tipo);
     else
-        k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk());
+        k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk(), tipo);
+}
+__global__ void k_potenziale_ibm(Geom g, const uint8_t* __restrict__ tipo, double* __restrict__ fi) {
+    k_potenziale_ibm_blk(g, tipo, fi, hw_blk());
 }
 __global__ void k_box_nonzero(long long n, const double* __restrict__ x, int* __restrict__ flag) {
     k_box_nonzero_blk(n, x, flag, hw_blk());
@@ -583,10 +588,11 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
             cudaMemsetAsync(xnz, 0, sizeof(int), h->st);
             k_box_nonzero<<<1216, 256, 0, h->st>>>(g.n, h->x, xnz);  // 8 CTAs per SM of a GB300
             k_resid_outer2_first<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b,
-                                                               xnz);
+                                                               xnz, h->tipo);
             ++h->launches;
         } else {
-            k_resid_outer2<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b);
+            k_resid_outer2<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b,
+                                                         h->tipo);
         }
         timed_end(h, KIND_OUTER, 1);
         k_reduce_final<<<1, 1024, 0, h->st>>>(h->part_a, h->part_b, nblk, h->red);
@@ -1100,6 +1106,19 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         }
     }
     if (d->solid && (rc = build_masks(h, d->solid))) return rc;
+    if (d->tipo) {  // cell types as a byte box: 0 solid, 1 IB, 2 fluid (>= 2), 3 anything else
+        const Geom& g1 = h->L[0].g;
+        std::vector<uint8_t> tb((size_t)g1.n, 3);
+        for (int k = 0; k <= jz + 1; ++k)
+            for (int j = 0; j <= jy + 1; ++j)
+                for (int i = 0; i <= jx + 1; ++i) {
+                    const int t = d->tipo[((size_t)k * (jy + 2) + j) * (jx + 2) + i];
+                    tb[(size_t)g1.at(i, j, k)] = t >= 2 ? 2 : (t == 1 ? 1 : (t == 0 ? 0 : 3));
+                }
+        if ((rc = dalloc(h, (void**)&h->tipo, (size_t)g1.n))) return rc;
+        CK(cudaMemcpyAsync(h->tipo, tb.data(), (size_t)g1.n, cudaMemcpyHostToDevice, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
     if ((rc = dalloc(h, (void**)&h->xn, nn * 8)) || (rc = dalloc(h, (void**)&h->yn, nn * 8)) ||
         (rc = dalloc(h, (void**)&h->zn, nn * 8)))
         return rc;
@@ -1820,6 +1839,24 @@ int ples_mg_project(ples_mg_handle* h, double* uc, double* vc, double* wc, doubl
         return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
     return with_device(h, [&]() -> int {
         return project_core(h, uc, vc, wc, u, v, w, fi, rel_tol, max_cycles, stats, false);
+    });
+}
+
+int ples_mg_potenziale_ibm(ples_mg_handle* h, double* fi) {
+    if (!h || !fi) return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    if (!h->tipo) return fail(h, PLES_MG_BAD_ARG, "the handle has no cell types (desc.tipo)");
+    return with_device(h, [&]() -> int {
+        const Geom& g = h->L[0].g;
+        const size_t ncell = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+        CK(cudaMemcpyAsync(h->fi_c, fi, 8 * ncell, cudaMemcpyHostToDevice, h->st));
+        k_compact_to_box<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->fi_c, h->x);
+        k_potenziale_ibm<<<dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz), dim3(32, 4), 0, h->st>>>(g, h->tipo, h->x);
+        k_box_to_compact<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->x, h->fi_c);
+        h->launches += 3;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(fi, h->fi_c, 8 * ncell, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        return PLES_MG_OK;
     });
 }
 

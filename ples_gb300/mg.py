@@ -41,7 +41,7 @@ class Desc(C.Structure):
                 ("z", C.POINTER(C.c_double)), ("dt", C.c_double), ("device", C.c_int),
                 ("nu_pre", C.c_int), ("nu_post", C.c_int), ("nu_coarse", C.c_int),
                 ("inner_cycles", C.c_int), ("smoother", C.c_int), ("coarsening", C.c_int),
-                ("solid", C.c_void_p)]
+                ("solid", C.c_void_p), ("tipo", C.c_void_p)]
 
 
 class Tuning(C.Structure):
@@ -70,7 +70,7 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_batch_solve", "ples_mg_batch_solve_device", "ples_mg_batch_info",
            "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
            "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune", "ples_mg_project",
-           "ples_mg_step", "ples_mg_residual_norms_device", "ples_mg_read_grid")
+           "ples_mg_step", "ples_mg_residual_norms_device", "ples_mg_read_grid", "ples_mg_potenziale_ibm")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -109,6 +109,7 @@ def load(build=True):
     L.ples_mg_project.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_step.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_read_grid.argtypes = [C.c_char_p, vp, vp, vp, vp, vp]
+    L.ples_mg_potenziale_ibm.argtypes = [vp, vp]
     L.ples_mg_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
     L.ples_mg_batch_solve.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
     L.ples_mg_batch_solve_device.argtypes = [vp, vp, vp, C.c_double, C.c_int, vp]
@@ -162,7 +163,7 @@ class Multigrid:
 
     def __init__(self, x, y, z, ip=0, jp=1, kp=0, precision="mixed", dt=1.0, device=0,
                  nlevmax=0, omega=0.0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0,
-                 smoother=0, coarsening=0, coords_layout=COORDS_NODES, solid=None):
+                 smoother=0, coarsening=0, coords_layout=COORDS_NODES, solid=None, tipo=None):
         self._L = load()
         self._x, self._y, self._z = _f64(x), _f64(y), _f64(z)
         if coords_layout == COORDS_NODES:
@@ -187,6 +188,12 @@ class Multigrid:
             if self._solid.shape != (jx, jy, jz):
                 raise ValueError(f"solid mask must be {(jx, jy, jz)}")
             d.solid = self._solid.ctypes.data
+        self._tipo = None
+        if tipo is not None:  # PLES cell types (jx+2, jy+2, jz+2): 0 solid, 1 IB, >= 2 fluid
+            self._tipo = np.asfortranarray(tipo, dtype=np.int32)
+            if self._tipo.shape != (jx + 2, jy + 2, jz + 2):
+                raise ValueError(f"tipo must be {(jx + 2, jy + 2, jz + 2)}")
+            d.tipo = self._tipo.ctypes.data
         h = C.c_void_p()
         rc = self._L.ples_mg_create(C.byref(d), C.byref(h))
         if rc != OK:
@@ -295,6 +302,15 @@ class Multigrid:
         self._check(rc, allow=(OK, NOT_CONVERGED))
         out = arrs[:4] + ([arrs[4], arrs[5], arrs[6]] if u is not None else [])
         return out, st.as_dict()
+
+    def potenziale_ibm(self, fi):
+        """Solid cells (tipo 0) of fi take the mean of their IB neighbours
+        (ples_mg_potenziale_ibm); returns a new array."""
+        a = _f64(fi).copy(order="F")
+        if a.shape != (self.jx + 2, self.jy + 2, self.jz + 2):
+            raise ValueError(f"fi of shape {a.shape}")
+        self._check(self._L.ples_mg_potenziale_ibm(self._h, C.c_void_p(a.ctypes.data)))
+        return a
 
     def step(self, u, v, w, uc, vc, wc, fi, rel_tol=1e-10, max_cycles=200):
         """The pressure step from the intermediate Cartesian velocities
