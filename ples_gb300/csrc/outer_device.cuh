@@ -54,32 +54,83 @@ __device__ __forceinline__ double flux_z(const Geom& g, const Coef<double>& c, c
 // r = b - L(x) with every face flux evaluated once and shared by its two
 // cells: the csi-face flux through the lane shuffle, the eta-face flux
 // through shared memory, the zeta-face flux carried while the thread walks
-// KC planes in k.  The FP64 pipe is the bound of this kernel, so sharing
-// roughly halves its time.  Per-block partial sum of squares and max |r|.
+// KC planes in k.  The cross terms use the central differences of the cells
+// on either side of a face, Dx = p(i+1)-p(i-1), Dy, Dz likewise: the four-
+// point bracket p(i+1,j+1)+p(i,j+1)-p(i+1,j-1)-p(i,j-1) of a csi face is
+// Dy(i+1) + Dy(i), and so on.  Each cell's three differences are formed
+// once and passed to its neighbours (lanes, shared memory, the next plane),
+// which takes about a third of the FP64 instructions out; the FP64 pipe is
+// the bound of this kernel.  Per-block partial sum of squares and max |r|.
 template <typename Ti, int KC>
 __device__ __forceinline__ void k_resid_outer2_blk(Geom g, Coef<double> c, const double* __restrict__ x,
                                                       const double* __restrict__ b, Ti* __restrict__ rin,
                                                       double* __restrict__ psq, double* __restrict__ pmax, const Blk& B,
                                                       const uint8_t* __restrict__ tipo = nullptr) {
-    __shared__ double sN[8][32];
+    __shared__ double sN[2][8][32], sDx[2][8][32], sDz[2][8][32];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i = B.x * 32 + tx + 1, j = B.y * 8 + ty + 1;
     const int k0 = B.z * KC + 1, k1 = min(k0 + KC - 1, g.nz);
     const bool act = i <= g.nx && j <= g.ny;
     const int ic = min(i, g.nx), jc = min(j, g.ny);  // keep idle threads' loads in the box
+    const long long sj = g.sj, sk = g.sk;
     double s = 0.0, m = 0.0;
-    double fB = flux_z(g, c, x, g.at(ic, jc, k0 - 1));
+    // differences of this thread's cell in plane k0 and the flux of its zeta face below
+    long long q = g.at(ic, jc, k0);
+    double Dx0 = x[q + 1] - x[q - 1], Dy0 = x[q + sj] - x[q - sj], Dz0 = x[q + sk] - x[q - sk];
+    double fB;
+    {
+        const long long qb = q - sk;
+        const double DxB = x[qb + 1] - x[qb - 1], DyB = x[qb + sj] - x[qb - sj];
+        fB = c.a3[qb] * (x[q] - x[qb]) + c.b31[qb] * (Dx0 + DxB) + c.b32[qb] * (Dy0 + DyB);
+    }
     for (int k = k0; k <= k1; ++k) {
-        const long long q = g.at(ic, jc, k);
-        const double fE = flux_x(g, c, x, q);
+        q = g.at(ic, jc, k);
+        const int buf = k & 1;
+        sDx[buf][ty][tx] = Dx0;
+        sDz[buf][ty][tx] = Dz0;
+        // the differences of plane k+1 (Dz only where a next step needs it)
+        const long long qf = q + sk;
+        const double Dx1 = x[qf + 1] - x[qf - 1], Dy1 = x[qf + sj] - x[qf - sj];
+        const double Dz1 = k < k1 ? x[qf + sk] - x[q] : 0.0;
+        // csi faces: east from the lane beside (lane 31 and the last column
+        // form their own), west by shuffle
+        double DyE = __shfl_down_sync(0xffffffffu, Dy0, 1), DzE = __shfl_down_sync(0xffffffffu, Dz0, 1);
+        if (tx == 31 || i + 1 > g.nx) {  // the lane beside holds no cell of its own
+            DyE = x[q + 1 + sj] - x[q + 1 - sj];
+            DzE = x[q + 1 + sk] - x[q + 1 - sk];
+        }
+        const double fE = c.a1[q] * (x[q + 1] - x[q]) + c.b12[q] * (DyE + Dy0) + c.b13[q] * (DzE + Dz0);
         double fW = __shfl_up_sync(0xffffffffu, fE, 1);
-        if (tx == 0) fW = flux_x(g, c, x, q - 1);
-        const double fN = flux_y(g, c, x, q);
-        sN[ty][tx] = fN;
+        if (tx == 0) {
+            const long long qw = q - 1;
+            const double DyW = x[qw + sj] - x[qw - sj], DzW = x[qw + sk] - x[qw - sk];
+            fW = c.a1[qw] * (x[q] - x[qw]) + c.b12[qw] * (Dy0 + DyW) + c.b13[qw] * (Dz0 + DzW);
+        }
         __syncthreads();
-        const double fS = ty > 0 ? sN[ty - 1][tx] : flux_y(g, c, x, q - g.sj);
+        // eta faces: north with the differences of the row above (shared
+        // memory; the last warp forms them), south from the warp below
+        double DxN, DzN;
+        if (ty < 7 && j + 1 <= g.ny) {  // the row above is a cell of this block
+            DxN = sDx[buf][ty + 1][tx];
+            DzN = sDz[buf][ty + 1][tx];
+        } else {
+            const long long qn = q + sj;
+            DxN = x[qn + 1] - x[qn - 1];
+            DzN = x[qn + sk] - x[qn - sk];
+        }
+        const double fN = c.a2[q] * (x[q + sj] - x[q]) + c.b21[q] * (DxN + Dx0) + c.b23[q] * (DzN + Dz0);
+        sN[buf][ty][tx] = fN;
         __syncthreads();
-        const double fF = flux_z(g, c, x, q);
+        double fS;
+        if (ty > 0) {
+            fS = sN[buf][ty - 1][tx];
+        } else {
+            const long long qs = q - sj;
+            const double DxS = x[qs + 1] - x[qs - 1], DzS = x[qs + sk] - x[qs - sk];
+            fS = c.a2[qs] * (x[q] - x[qs]) + c.b21[qs] * (Dx0 + DxS) + c.b23[qs] * (Dz0 + DzS);
+        }
+        // zeta face above
+        const double fF = c.a3[q] * (x[qf] - x[q]) + c.b31[q] * (Dx1 + Dx0) + c.b32[q] * (Dy1 + Dy0);
         if (act) {
             const double r = b[q] - ((fE - fW) + (fN - fS) + (fF - fB));
             rin[q] = Ti(r);
@@ -87,6 +138,9 @@ __device__ __forceinline__ void k_resid_outer2_blk(Geom g, Coef<double> c, const
             if (!tipo || tipo[q] == 2) m = fmax(m, fabs(r));  // max over fluid cells (tipo >= 2)
         }
         fB = fF;
+        Dx0 = Dx1;
+        Dy0 = Dy1;
+        Dz0 = Dz1;
     }
     block_reduce_sum_max(s, m);
     if (threadIdx.x == 0) {

@@ -234,7 +234,9 @@ def test_staged_and_plain_zebra_agree(case0):
 
 
 def test_odd_level_counts_and_small_grids():
-    for dims in ((48, 32, 48), (16, 8, 16), (32, 64, 32)):
+    # (40, 12, 20): partial 32-lane tiles, rows not a multiple of the 8-row
+    # blocks and planes not a multiple of the 8-plane walks of the kernels
+    for dims in ((48, 32, 48), (16, 8, 16), (32, 64, 32), (40, 12, 20)):
         x, y, z = S.wavy_channel_grid(*dims, 0.05, 1.5)
         rhs = S.divergence_rhs(*dims, seed=3)
         orc = Oracle(x, y, z, islor=1)
