@@ -745,14 +745,21 @@ double mean_spacing(const double* x, const double* y, const double* z, int jx, i
 }
 
 // Gauss-Jordan inversion with partial pivoting on the device (FP64), one
-// pivot column per step over the m x m matrix K and its inverse I:
+// pivot column per step.  K (m x m) is reduced to the identity while the
+// same row operations build its inverse E.  E is kept with its columns in
+// pivot order, S(:,c) = E(:,perm(c)) for the original row perm(c) chosen at
+// step c: before its step a column of E is a unit vector that need not be
+// stored, so step col works on the K columns after col and the S columns up
+// to col only, m per row in all.
 //   k_gj_pivot      one CTA: the row p >= col of largest |K(p,col)|; keeps
 //                   K(p,col) and K(col,col) for the step
-//   k_gj_swap_scale thread t: rows p and col swapped in column t, the pivot
-//                   row scaled by 1/K(p,col); the elimination factors
-//                   f(r) = K(r,col) after the swap (0 for the pivot row)
-//   k_gj_eliminate  K(r,q) -= f(r) K(col,q) (q >= col; the columns before
-//                   are unit columns already) and I(r,q) -= f(r) I(col,q)
+//   k_gj_swap_scale thread t: rows p and col swapped in K column t >= col
+//                   and S column t < col, the pivot row scaled by
+//                   1/K(p,col); the elimination factors f(r) = K(r,col)
+//                   after the swap (0 for the pivot row); perm updated
+//   k_gj_eliminate  one CTA per row r with f(r) != 0: K(r,q) -= f(r) K(col,q)
+//                   for q > col, S(r,c) -= f(r) S(col,c) for c < col, and
+//                   the new column S(r,col) = -f(r) / K(p,col)
 struct GjStep {
     int piv;
     int bad;
@@ -789,38 +796,55 @@ __global__ void k_gj_pivot(const double* __restrict__ K, int m, int col, GjStep*
         st->kcc = K[(size_t)col * m + col];
     }
 }
-__global__ void k_gj_swap_scale(double* __restrict__ K, double* __restrict__ I, double* __restrict__ f, int m,
-                                int col, const GjStep* st) {
+__global__ void k_gj_swap_scale(double* __restrict__ K, double* __restrict__ S, double* __restrict__ f,
+                                int* __restrict__ perm, int m, int col, const GjStep* st) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m || st->bad) return;
     const int p = st->piv;
     const double inv = 1.0 / st->pv;
     // factor of row t after the swap (rows other than p and col keep theirs)
     f[t] = t == col ? 0.0 : (t == p ? st->kcc : K[(size_t)t * m + col]);
-    const double ka = K[(size_t)p * m + t], kb = K[(size_t)col * m + t];
-    const double ia = I[(size_t)p * m + t], ib = I[(size_t)col * m + t];
-    if (p != col) {
-        K[(size_t)p * m + t] = kb;
-        I[(size_t)p * m + t] = ib;
+    if (t >= col) {
+        const double ka = K[(size_t)p * m + t], kb = K[(size_t)col * m + t];
+        if (p != col) K[(size_t)p * m + t] = kb;
+        K[(size_t)col * m + t] = ka * inv;
     }
-    K[(size_t)col * m + t] = ka * inv;
-    I[(size_t)col * m + t] = ia * inv;
+    if (t < col) {
+        const double sa = S[(size_t)p * m + t], sb = S[(size_t)col * m + t];
+        if (p != col) S[(size_t)p * m + t] = sb;
+        S[(size_t)col * m + t] = sa * inv;
+    } else if (t == col) {
+        S[(size_t)col * m + col] = inv;  // the unit column of the pivot row, scaled
+        if (p != col) {
+            const int o = perm[p];
+            perm[p] = perm[col];
+            perm[col] = o;
+        }
+    }
 }
-__global__ void k_gj_eliminate(double* __restrict__ K, double* __restrict__ I, const double* __restrict__ f, int m,
+__global__ void k_gj_eliminate(double* __restrict__ K, double* __restrict__ S, const double* __restrict__ f, int m,
                                int col, const GjStep* st) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r = blockIdx.y;
-    if (q >= m || r == col || st->bad) return;
+    const int r = blockIdx.x;
+    if (r == col || st->bad) return;
     const double fr = f[r];
     if (fr == 0.0) return;
-    if (q >= col) K[(size_t)r * m + q] -= fr * K[(size_t)col * m + q];
-    I[(size_t)r * m + q] -= fr * I[(size_t)col * m + q];
+    double* Kr = K + (size_t)r * m;
+    const double* Kc = K + (size_t)col * m;
+    for (int q = col + 1 + (int)threadIdx.x; q < m; q += blockDim.x) Kr[q] -= fr * Kc[q];
+    double* Sr = S + (size_t)r * m;
+    const double* Sc = S + (size_t)col * m;
+    for (int c = threadIdx.x; c < col; c += blockDim.x) Sr[c] -= fr * Sc[c];
+    if (threadIdx.x == 0) Sr[col] = -fr / st->pv;
 }
+// the inverse of the bordered system without its border: Inv(r, perm(c)) = S(r, c)
 template <typename T>
-__global__ void k_gj_extract(const double* __restrict__ I, int m, int n, T* __restrict__ S) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_gj_extract(const double* __restrict__ S, const int* __restrict__ perm, int m, int n,
+                             T* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = blockIdx.y;
-    if (q < n) S[(size_t)r * n + q] = T(I[(size_t)r * m + q]);
+    if (c >= m) return;
+    const int o = perm[c];
+    if (o < n) out[(size_t)r * n + o] = T(S[(size_t)r * m + c]);
 }
 
 // dense inverse of the bordered coarsest system [[M, v], [1^T, 0]] (M: the
@@ -916,8 +940,8 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         }
     }
     // Gauss-Jordan inverse with partial pivoting, on the device
-    std::vector<double> I((size_t)m * m, 0.0);
-    for (int u = 0; u < m; ++u) I[(size_t)u * m + u] = 1.0;
+    std::vector<int> perm0(m);
+    for (int u = 0; u < m; ++u) perm0[u] = u;
     std::vector<void*> tmp;
     auto talloc = [&](void** p, size_t bytes) -> int {
         if (cudaMalloc(p, bytes) != cudaSuccess) {
@@ -929,20 +953,23 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         return PLES_MG_OK;
     };
     double *dK, *dI, *dF;
+    int* dP;
     GjStep* dS;
     int rc;
     if ((rc = talloc((void**)&dK, 8 * (size_t)m * m)) || (rc = talloc((void**)&dI, 8 * (size_t)m * m)) ||
-        (rc = talloc((void**)&dF, 8 * (size_t)m)) || (rc = talloc((void**)&dS, sizeof(GjStep))))
+        (rc = talloc((void**)&dF, 8 * (size_t)m)) || (rc = talloc((void**)&dP, sizeof(int) * (size_t)m)) ||
+        (rc = talloc((void**)&dS, sizeof(GjStep))))
         return rc;
     auto gj = [&]() -> int {
         CK(cudaMemcpyAsync(dK, K.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
-        CK(cudaMemcpyAsync(dI, I.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemsetAsync(dI, 0, 8 * (size_t)m * m, h->st));
+        CK(cudaMemcpyAsync(dP, perm0.data(), sizeof(int) * (size_t)m, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemsetAsync(dS, 0, sizeof(GjStep), h->st));
         const int tb = 256, nb = (m + tb - 1) / tb;
         for (int col = 0; col < m; ++col) {
             k_gj_pivot<<<1, 1024, 0, h->st>>>(dK, m, col, dS);
-            k_gj_swap_scale<<<nb, tb, 0, h->st>>>(dK, dI, dF, m, col, dS);
-            k_gj_eliminate<<<dim3(nb, m), tb, 0, h->st>>>(dK, dI, dF, m, col, dS);
+            k_gj_swap_scale<<<nb, tb, 0, h->st>>>(dK, dI, dF, dP, m, col, dS);
+            k_gj_eliminate<<<m, tb, 0, h->st>>>(dK, dI, dF, m, col, dS);
         }
         h->launches += 3LL * m;
         CK(cudaGetLastError());
@@ -951,7 +978,7 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         CK(cudaStreamSynchronize(h->st));
         if (hs.bad) return fail(h, PLES_MG_BAD_ARG, "coarsest-level system is singular");
         if ((rc = dalloc(h, &h->coarse_S, sizeof(T) * (size_t)n * n))) return rc;
-        k_gj_extract<T><<<dim3((n + 255) / 256, n), 256, 0, h->st>>>(dI, m, n, (T*)h->coarse_S);
+        k_gj_extract<T><<<dim3((m + 255) / 256, n), 256, 0, h->st>>>(dI, dP, m, n, (T*)h->coarse_S);
         ++h->launches;
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(h->st));
