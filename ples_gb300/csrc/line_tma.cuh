@@ -76,8 +76,8 @@ __global__ void __launch_bounds__(256) k_line_relax_tma(const __grid_constant__ 
                                                         const float* __restrict__ pin, float* pout, float omega,
                                                         int kpar, int zk, int pin_is_a, int pk_is_a,
                                                         int* __restrict__ err) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* buf = reinterpret_cast<float*>(smem_raw);
+    extern __shared__ __align__(128) unsigned char smem_tma[];
+    float* buf = reinterpret_cast<float*>(smem_tma);
     const int nj = g.ny + 2, ny = g.ny;
     float* G = buf + kNB * ChunkLayout::SIZE;
     float* AL = G + nj * 32;
@@ -95,7 +95,6 @@ __global__ void __launch_bounds__(256) k_line_relax_tma(const __grid_constant__ 
     const int i = i0 + lane + 1;
     const bool act = i <= g.nx;
     const bool odd = i & 1;  // updated in the second half
-    const long long sj = g.sj, sk = g.sk;
     const int nchunk = (nj + kRC - 1) / kRC;
     const CUtensorMap* mpin = pin_is_a ? &maps.pA : &maps.pB;
     const CUtensorMap* mpk = pk_is_a ? &maps.pA : &maps.pB;

@@ -1952,7 +1952,7 @@ int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) 
             return PLES_MG_OK;
         };
         int rc, tried = 0;
-        double ms;
+        double ms = 0.0;
         ples_mg_stats st;
         const int nsmooth = h->coarse_S ? h->nlev - 1 : h->nlev;
         for (int n = 0; n < nsmooth; ++n) {
