@@ -648,6 +648,7 @@ int batch_create(ples_mg_handle* const* members, int n, ples_mg_batch* b) {
                          "member %d: batched solves need mixed precision, the zebra smoother and full coarsening", i);
         if (!h->coarse_S) return bfail(b, PLES_MG_BAD_ARG, "member %d: coarsest level too large for the dense solve", i);
         if (h->masked) return bfail(b, PLES_MG_BAD_ARG, "member %d: immersed-boundary masks are not batched", i);
+        if (h->walls_xz) return bfail(b, PLES_MG_BAD_ARG, "member %d: x or z walls are not batched", i);
         if (h->tipo) return bfail(b, PLES_MG_BAD_ARG, "member %d: cell types (tipo) are not batched", i);
         if (h->nu_pre != h->nu_post)
             return bfail(b, PLES_MG_BAD_ARG, "member %d: batched solves need nu_pre == nu_post", i);

@@ -46,6 +46,8 @@ struct ples_mg_handle {
     double *xn = nullptr, *yn = nullptr, *zn = nullptr;  // fine nodes (0:jx,0:jy,0:jz)
     double *x = nullptr, *b = nullptr;                   // FP64 solution / rhs boxes (level 1)
     double* wbuf = nullptr;                              // 2*nx*nz wall rows
+    void* sbuf = nullptr;                                // ghosts of walled x/z directions (side_cells, 8 B each)
+    bool walls_xz = false;                               // ip = 1 or kp = 1
     double *part_a = nullptr, *part_b = nullptr;         // block partials
     long long npart = 0;
     double* red = nullptr;                               // 2 doubles on the device (+ dflag)

@@ -49,6 +49,7 @@ struct Geom {
     int sj;          // row pitch (elements)
     long long sk;    // plane pitch (elements)
     long long n;     // elements in the box allocation
+    int px, pz;      // 1: periodic in x / z (ghosts are images); 0: walls (ghosts from their relation)
     __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
         return (long long)k * sk + (long long)j * sj + (long long)(i + kOX);
     }
@@ -61,6 +62,7 @@ inline Geom make_geom(int nx, int ny, int nz) {
     g.sj = (need + 31) / 32 * 32;
     g.sk = (long long)g.sj * (ny + 2);
     g.n = g.sk * (nz + 2);
+    g.px = g.pz = 1;
     return g;
 }
 
@@ -111,18 +113,18 @@ __device__ __forceinline__ void pf_l2(const T* p, unsigned q) {
 template <typename T>
 __device__ __forceinline__ void store_periodic(const Geom& g, T* p, int i, int j, int k, T v) {
     p[g.at(i, j, k)] = v;
-    const int gi = i == g.nx ? 0 : (i == 1 ? g.nx + 1 : -1);
-    const int gk = k == g.nz ? 0 : (k == 1 ? g.nz + 1 : -1);
+    const int gi = !g.px ? -1 : (i == g.nx ? 0 : (i == 1 ? g.nx + 1 : -1));
+    const int gk = !g.pz ? -1 : (k == g.nz ? 0 : (k == 1 ? g.nz + 1 : -1));
     if (gi >= 0) p[g.at(gi, j, k)] = v;
     if (gk >= 0) {
         p[g.at(i, j, gk)] = v;
         if (gi >= 0) p[g.at(gi, j, gk)] = v;
     }
-    if (g.nx == 1 && i == 1) {  // a single column is its own image on both sides
+    if (g.px && g.nx == 1 && i == 1) {  // a single column is its own image on both sides
         p[g.at(0, j, k)] = v;
         if (gk >= 0) p[g.at(0, j, gk)] = v;
     }
-    if (g.nz == 1 && k == 1) {
+    if (g.pz && g.nz == 1 && k == 1) {
         p[g.at(i, j, 0)] = v;
         if (gi >= 0) p[g.at(gi, j, 0)] = v;
     }
@@ -182,7 +184,11 @@ __device__ __forceinline__ void k_ghost_xz_blk(Geom g, T* __restrict__ p, const 
             j = (int)(r - (long long)(k - 1) * nyg);
             i = side ? g.nx + 1 : 0;
         }
-        int si = i == 0 ? g.nx : (i == g.nx + 1 ? 1 : i);
+        // walled directions keep their ghosts (set by their relations); at
+        // a periodic z plane a wall column takes the image of its own column
+        const bool xg = i == 0 || i == g.nx + 1, zg = k == 0 || k == g.nz + 1;
+        if ((xg && !g.px && !zg) || (zg && !g.pz)) continue;
+        int si = g.px ? (i == 0 ? g.nx : (i == g.nx + 1 ? 1 : i)) : i;
         int sk = k == 0 ? g.nz : (k == g.nz + 1 ? 1 : k);
         p[g.at(i, j, k)] = p[g.at(si, j, sk)];
     }

@@ -294,9 +294,165 @@ __device__ __forceinline__ void k_wall_scatter_blk(Geom g, double* __restrict__ 
     const int k = B.y * blockDim.y + threadIdx.y;
     const int side = B.z;
     if (i > g.nx + 1 || k > g.nz + 1) return;
+    // the edge cells of a walled direction follow their own copy rules (side fill)
+    if ((!g.px && (i == 0 || i == g.nx + 1)) || (!g.pz && (k == 0 || k == g.nz + 1))) return;
     const int wi = i == 0 ? g.nx : (i == g.nx + 1 ? 1 : i);
     const int wk = k == 0 ? g.nz : (k == g.nz + 1 ? 1 : k);
     p[g.at(i, side ? g.ny + 1 : 0, k)] = w[(long long)side * g.nx * g.nz + (long long)(wk - 1) * g.nx + (wi - 1)];
+}
+// ---------------------------------------------------------------------------
+// Ghost cells of a walled x or z direction (ip = 1 / kp = 1): the face
+// relations of mul_boun_sndrcv (multigrid.f03:1111-1158 left/right,
+// 1280-1316 back/front; the flux through the wall face equals an*cs/dt) and
+// its edge copies (:1360-1742).  k_side_compute evaluates every face ghost
+// from the current field into w (Jacobi), k_side_scatter writes them (also
+// into p2 when given: the zebra's second launch reads its k+-1 planes from
+// the output buffer) with their images in a periodic direction, and
+// k_side_edges sets the edge cells.  With zero set the ghosts become 0 (a
+// correction that starts from zero).
+// w: x walls [side][k-1][j-1] (2 ny nz), then z walls [side][j-1][i-1] (2 nx ny)
+__host__ __device__ __forceinline__ long long side_cells(const Geom& g) {
+    return (g.px ? 0 : 2LL * g.ny * g.nz) + (g.pz ? 0 : 2LL * g.nx * g.ny);
+}
+template <typename T>
+__device__ __forceinline__ void k_side_compute_blk(Geom g, Coef<T> c, const T* __restrict__ p, T* __restrict__ w,
+                                                   const double* __restrict__ cs1, const double* __restrict__ cs2,
+                                                   const double* __restrict__ cs5, const double* __restrict__ cs6,
+                                                   double an_dt, int zero, const Blk& B) {
+    const long long nxw = g.px ? 0 : 2LL * g.ny * g.nz;
+    const long long t = (long long)B.x * blockDim.x + threadIdx.x;
+    if (t >= side_cells(g)) return;
+    if (zero) {
+        w[t] = T(0);
+        return;
+    }
+    const long long sj = g.sj, sk = g.sk;
+    if (t < nxw) {
+        const long long per = (long long)g.ny * g.nz;
+        const int side = (int)(t / per);
+        const long long r = t - side * per;
+        const int k = (int)(r / g.ny) + 1, j = (int)(r % g.ny) + 1;
+        const long long ci = (long long)(k - 1) * g.ny + (j - 1);
+        if (side == 0) {
+            const long long q0 = g.at(0, j, k), q1 = q0 + 1;
+            const T a = c.a1[q0];
+            T v = p[q1];
+            if (cs1) v -= T(an_dt * cs1[ci]) / a;
+            v += (c.b12[q0] * (p[q1 + sj] + p[q0 + sj] - p[q1 - sj] - p[q0 - sj]) +
+                  c.b13[q0] * (p[q1 + sk] + p[q0 + sk] - p[q1 - sk] - p[q0 - sk])) / a;
+            w[t] = v;
+        } else {
+            const long long qt = g.at(g.nx + 1, j, k), qn = qt - 1;
+            const T a = c.a1[qn];
+            T v = p[qn];
+            if (cs2) v += T(an_dt * cs2[ci]) / a;
+            v -= (c.b12[qn] * (p[qt + sj] + p[qn + sj] - p[qt - sj] - p[qn - sj]) +
+                  c.b13[qn] * (p[qt + sk] + p[qn + sk] - p[qt - sk] - p[qn - sk])) / a;
+            w[t] = v;
+        }
+    } else {
+        const long long per = (long long)g.nx * g.ny, u = t - nxw;
+        const int side = (int)(u / per);
+        const long long r = u - side * per;
+        const int j = (int)(r / g.nx) + 1, i = (int)(r % g.nx) + 1;
+        const long long ci = (long long)(j - 1) * g.nx + (i - 1);
+        if (side == 0) {
+            const long long q0 = g.at(i, j, 0), q1 = q0 + sk;
+            const T a = c.a3[q0];
+            T v = p[q1];
+            if (cs5) v -= T(an_dt * cs5[ci]) / a;
+            v += (c.b31[q0] * (p[q1 + 1] + p[q0 + 1] - p[q1 - 1] - p[q0 - 1]) +
+                  c.b32[q0] * (p[q1 + sj] + p[q0 + sj] - p[q1 - sj] - p[q0 - sj])) / a;
+            w[t] = v;
+        } else {
+            const long long qt = g.at(i, j, g.nz + 1), qn = qt - sk;
+            const T a = c.a3[qn];
+            T v = p[qn];
+            if (cs6) v += T(an_dt * cs6[ci]) / a;
+            v -= (c.b31[qn] * (p[qt + 1] + p[qn + 1] - p[qt - 1] - p[qn - 1]) +
+                  c.b32[qn] * (p[qt + sj] + p[qn + sj] - p[qt - sj] - p[qn - sj])) / a;
+            w[t] = v;
+        }
+    }
+}
+template <typename T>
+__device__ __forceinline__ void k_side_scatter_blk(Geom g, T* __restrict__ p, T* __restrict__ p2,
+                                                   const T* __restrict__ w, const Blk& B) {
+    const long long nxw = g.px ? 0 : 2LL * g.ny * g.nz;
+    const long long t = (long long)B.x * blockDim.x + threadIdx.x;
+    if (t >= side_cells(g)) return;
+    const T v = w[t];
+    auto put = [&](int i, int j, int k) {
+        const long long q = g.at(i, j, k);
+        p[q] = v;
+        if (p2) p2[q] = v;
+    };
+    if (t < nxw) {
+        const long long per = (long long)g.ny * g.nz;
+        const int side = (int)(t / per);
+        const long long r = t - side * per;
+        const int k = (int)(r / g.ny) + 1, j = (int)(r % g.ny) + 1;
+        const int i = side ? g.nx + 1 : 0;
+        put(i, j, k);
+        if (g.pz && k == g.nz) put(i, j, 0);
+        if (g.pz && k == 1) put(i, j, g.nz + 1);
+    } else {
+        const long long per = (long long)g.nx * g.ny, u = t - nxw;
+        const int side = (int)(u / per);
+        const long long r = u - side * per;
+        const int j = (int)(r / g.nx) + 1, i = (int)(r % g.nx) + 1;
+        const int k = side ? g.nz + 1 : 0;
+        put(i, j, k);
+        if (g.px && i == g.nx) put(0, j, k);
+        if (g.px && i == 1) put(g.nx + 1, j, k);
+    }
+}
+// one CTA; the stages follow the reference's order, each reading what the
+// one before wrote
+template <typename T>
+__device__ __forceinline__ void k_side_edges_blk(Geom g, T* __restrict__ p, T* __restrict__ p2, int zero) {
+    auto cp = [&](int i, int j, int k, int si, int sj2, int sk2) {
+        const T v = zero ? T(0) : p[g.at(si, sj2, sk2)];
+        p[g.at(i, j, k)] = v;
+        if (p2) p2[g.at(i, j, k)] = v;
+    };
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (g.pz) {  // z periodic: the horizontal square of x walls, z images included (:1420-1460)
+        if (g.px) return;
+        for (int k = threadIdx.x; k <= nz + 1; k += blockDim.x) {
+            cp(0, ny + 1, k, 0, ny, k);
+            cp(0, 0, k, 0, 1, k);
+            cp(nx + 1, ny + 1, k, nx + 1, ny, k);
+            cp(nx + 1, 0, k, nx + 1, 1, k);
+        }
+        return;
+    }
+    // z walls (:1628-1742): the wall planes' y edges, then their x edges, then
+    // the horizontal square of x walls
+    for (int t = threadIdx.x; t < 2 * nx; t += blockDim.x) {
+        const int i = t % nx + 1, kg = t < nx ? 0 : nz + 1;
+        cp(i, 0, kg, i, 1, kg);
+        cp(i, ny + 1, kg, i, ny, kg);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 2 * (ny + 2); t += blockDim.x) {
+        const int j = t % (ny + 2), kg = t < ny + 2 ? 0 : nz + 1;
+        if (g.px) {
+            cp(0, j, kg, nx, j, kg);
+            cp(nx + 1, j, kg, 1, j, kg);
+        } else {
+            cp(0, j, kg, 1, j, kg);
+            cp(nx + 1, j, kg, nx, j, kg);
+        }
+    }
+    __syncthreads();
+    if (!g.px)
+        for (int k = 1 + threadIdx.x; k <= nz; k += blockDim.x) {
+            cp(0, ny + 1, k, 1, ny + 1, k);
+            cp(0, 0, k, 1, 0, k);
+            cp(nx + 1, ny + 1, k, nx, ny + 1, k);
+            cp(nx + 1, 0, k, nx, 0, k);
+        }
 }
 // compact Fortran arrays <-> ghosted boxes
 __device__ __forceinline__ void k_compact_to_box_blk(Geom g, int ghost, const double* __restrict__ src, double* __restrict__ dst, const Blk& B) {

@@ -118,6 +118,21 @@ __global__ void k_wall_scatter(Geom g, double* __restrict__ p, const double* __r
     k_wall_scatter_blk(g, p, w, hw_blk());
 }
 
+template <typename T>
+__global__ void k_side_compute(Geom g, Coef<T> c, const T* __restrict__ p, T* __restrict__ w,
+                               const double* __restrict__ cs1, const double* __restrict__ cs2,
+                               const double* __restrict__ cs5, const double* __restrict__ cs6, double an_dt, int zero) {
+    k_side_compute_blk<T>(g, c, p, w, cs1, cs2, cs5, cs6, an_dt, zero, hw_blk());
+}
+template <typename T>
+__global__ void k_side_scatter(Geom g, T* __restrict__ p, T* __restrict__ p2, const T* __restrict__ w) {
+    k_side_scatter_blk<T>(g, p, p2, w, hw_blk());
+}
+template <typename T>
+__global__ void k_side_edges(Geom g, T* __restrict__ p, T* __restrict__ p2, int zero) {
+    k_side_edges_blk<T>(g, p, p2, zero);
+}
+
 // contraction factor of the Jacobi wall fill: max 2(|B21|+|B23|)/A2
 __global__ void k_wall_contraction(Geom g, Coef<double> c, unsigned long long* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -375,6 +390,21 @@ int build_line_maps(ples_mg_handle* h, LevelData& L) {
 }
 
 // nu sweeps; `zero` = the field is identically zero before the first sweep
+// one pass of the ghost relations of walled x / z directions (and their
+// edges) over p, written to p and p2; zero: all those ghosts become 0
+template <typename T>
+void side_fill(ples_mg_handle* h, const Geom& g, const Coef<T>& c, T* p, T* p2, const double* const cs[6],
+               double an_dt, bool zero) {
+    const long long n = side_cells(g);
+    if (n == 0) return;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    k_side_compute<T><<<nb, 256, 0, h->st>>>(g, c, p, (T*)h->sbuf, cs ? cs[0] : nullptr, cs ? cs[1] : nullptr,
+                                             cs ? cs[4] : nullptr, cs ? cs[5] : nullptr, an_dt, zero ? 1 : 0);
+    k_side_scatter<T><<<nb, 256, 0, h->st>>>(g, p, p2, (const T*)h->sbuf);
+    k_side_edges<T><<<1, 256, 0, h->st>>>(g, p, p2, zero ? 1 : 0);
+    h->launches += 3;
+}
+
 template <typename T>
 void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
     if (zero && nu == 0) cudaMemsetAsync(L.p, 0, sizeof(T) * (size_t)L.g.n, h->st);
@@ -383,8 +413,12 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
     const int nt = h->smoother == 1 ? std::min(L.line_threads, 256) : L.line_threads;
     const size_t smem = line_smem<T>(L.g, nt);
     const T* cp = (const T*)L.cp;
+    const bool walls = !L.g.px || !L.g.pz;
     for (int s = 0; s < nu; ++s) {
         const bool zin = zero && s == 0;
+        // ghosts of walled x / z directions from the field about to be relaxed
+        // (zeros for a correction starting from zero), in both buffers
+        if (walls) side_fill<T>(h, L.g, c, (T*)L.p, (T*)L.p2, nullptr, 0.0, zin);
         const T* pin = (const T*)L.p;
         T* pout = (T*)L.p2;
         timed_begin(h, KIND_LINE, level);
@@ -428,6 +462,7 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
         timed_end(h, KIND_LINE, level);
         std::swap(L.p, L.p2);
     }
+    if (walls && nu > 0) side_fill<T>(h, L.g, c, (T*)L.p, (T*)L.p2, nullptr, 0.0, false);
 }
 
 template <typename T>
@@ -513,16 +548,17 @@ int sum_interior(ples_mg_handle* h, const double* a, int squares, double* out) {
 // wall ghost rows of p driven towards the fixed point of their relation
 // (Jacobi passes); the x/z ghost shell of the interior rows must already be
 // consistent, the scatter maintains it for the wall rows
-void wall_fill(ples_mg_handle* h, double* p, const double* cs3, const double* cs4, double an_dt, int passes,
-               const Geom& g, const Coef<double>& c) {
+void wall_fill(ples_mg_handle* h, double* p, const double* const cs[6], double an_dt, int passes, const Geom& g,
+               const Coef<double>& c) {
     dim3 blk(32, 4);
     for (int s = 0; s < passes; ++s) {
         timed_begin(h, KIND_WALL, 1);
-        k_wall_compute<<<dim3((g.nx + 31) / 32, (g.nz + 3) / 4, 2), blk, 0, h->st>>>(g, c, p, h->wbuf, cs3, cs4,
-                                                                                    an_dt);
+        k_wall_compute<<<dim3((g.nx + 31) / 32, (g.nz + 3) / 4, 2), blk, 0, h->st>>>(
+            g, c, p, h->wbuf, cs ? cs[2] : nullptr, cs ? cs[3] : nullptr, an_dt);
         k_wall_scatter<<<dim3((g.nx + 2 + 31) / 32, (g.nz + 2 + 3) / 4, 2), blk, 0, h->st>>>(g, p, h->wbuf);
-        timed_end(h, KIND_WALL, 1);
         h->launches += 2;
+        side_fill<double>(h, g, c, p, nullptr, cs, an_dt, false);
+        timed_end(h, KIND_WALL, 1);
     }
 }
 
@@ -546,20 +582,24 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     double sb = 0.0;
     int rc = sum_interior(h, h->b, 0, &sb);
     if (rc) return rc;
+    // net flux through the walls: (cs2 - cs1) + (cs4 - cs3) + (cs6 - cs5), over dt
     double flux = 0.0;
-    if (h->cs_c[2] || h->cs_c[3]) {
-        double s3 = 0.0, s4 = 0.0;
-        for (int side = 0; side < 2; ++side) {
-            const double* a = h->cs_c[2 + side];
+    {
+        const long long nf[6] = {(long long)g.ny * g.nz, (long long)g.ny * g.nz, (long long)g.nx * g.nz,
+                                 (long long)g.nx * g.nz, (long long)g.nx * g.ny, (long long)g.nx * g.ny};
+        double sum[6] = {0, 0, 0, 0, 0, 0};
+        bool any = false;
+        for (int s = 0; s < 6; ++s) {
+            const double* a = h->cs_c[s];
             if (!a) continue;
-            long long n = (long long)g.nx * g.nz;
-            k_reduce_final<<<1, 1024, 0, h->st>>>(a, nullptr, n, h->red);
+            any = true;
+            k_reduce_final<<<1, 1024, 0, h->st>>>(a, nullptr, nf[s], h->red);
             ++h->launches;
             CK(cudaMemcpyAsync(h->h_red, h->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
             CK(cudaStreamSynchronize(h->st));
-            (side ? s4 : s3) = h->h_red[0];
+            sum[s] = h->h_red[0];
         }
-        flux = (s4 - s3) / dt;
+        if (any) flux = ((sum[1] - sum[0]) + (sum[3] - sum[2]) + (sum[5] - sum[4])) / dt;
     }
     const double shift = (sb - flux) / N;
     {
@@ -581,7 +621,7 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     // its wall fill) with its norms copied to h_red, preceded from the second
     // test on by the V-cycles and the update
     auto enqueue_residual = [&](bool first) {
-        wall_fill(h, h->x, h->cs_c[2], h->cs_c[3], 1.0 / dt, h->wall_passes, g, F.cd);
+        wall_fill(h, h->x, h->cs_c, 1.0 / dt, h->wall_passes, g, F.cd);
         timed_begin(h, KIND_OUTER, 1);
         if (first) {  // a zero initial guess needs no stencil
             int* xnz = reinterpret_cast<int*>(h->red + 5);
@@ -611,8 +651,10 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     if (graphs) {
         std::vector<long long> key = {(long long)sizeof(T), h->inner_cycles, h->nu_pre, h->nu_post, h->nu_coarse,
                                       h->timed_kind, h->timed_level,
-                                      h->smoother, h->wall_passes, (long long)(uintptr_t)h->cs_c[2],
-                                      (long long)(uintptr_t)h->cs_c[3]};
+                                      h->smoother, h->wall_passes, (long long)(uintptr_t)h->cs_c[0],
+                                      (long long)(uintptr_t)h->cs_c[1], (long long)(uintptr_t)h->cs_c[2],
+                                      (long long)(uintptr_t)h->cs_c[3], (long long)(uintptr_t)h->cs_c[4],
+                                      (long long)(uintptr_t)h->cs_c[5]};
         double an = 1.0 / dt;
         long long anb;
         std::memcpy(&anb, &an, sizeof anb);
@@ -706,8 +748,10 @@ int validate(const ples_mg_desc* d, ples_mg_handle* h) {
     if (!d) return fail(h, PLES_MG_BAD_ARG, "null descriptor");
     if (d->jx < 8 || d->jy < 4 || d->jz < 8) return fail(h, PLES_MG_BAD_ARG, "grid too small (jx,jz >= 8, jy >= 4)");
     if (d->jp != 1) return fail(h, PLES_MG_BAD_ARG, "y-periodic grids are not supported (jp must be 1)");
-    if (d->ip != 0 || d->kp != 0)
-        return fail(h, PLES_MG_BAD_ARG, "x or z walls (ip/kp = 1) are not supported on the device");
+    if ((d->ip != 0 && d->ip != 1) || (d->kp != 0 && d->kp != 1))
+        return fail(h, PLES_MG_BAD_ARG, "ip and kp must be 0 (periodic) or 1 (walls)");
+    if ((d->ip || d->kp) && d->solid)
+        return fail(h, PLES_MG_BAD_ARG, "an immersed-boundary mask needs periodic x and z (ip = kp = 0)");
     if (d->precision != PLES_MG_PREC_FP64 && d->precision != PLES_MG_PREC_MIXED)
         return fail(h, PLES_MG_BAD_ARG, "unknown precision %d", d->precision);
     if (d->coords_layout != PLES_MG_COORDS_NODES && d->coords_layout != PLES_MG_COORDS_GHOSTED8)
@@ -1104,7 +1148,7 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         const bool can_z = nz % 2 == 0 && nz / 2 >= 2;
         if (!can_y) break;
         // automatic depth: the dense coarsest solve from the first level small enough
-        if (d->nlevmax == 0 && nl >= 2 && (long long)nx * nz * (ny + 2) <= kDenseMax) break;
+        if (d->nlevmax == 0 && nl >= 2 && !d->ip && !d->kp && (long long)nx * nz * (ny + 2) <= kDenseMax) break;
         int rx, rz;
         if (d->coarsening == 0) {
             if (!can_x || !can_z) break;
@@ -1122,6 +1166,11 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         ++nl;
     }
     h->nlev = nl;
+    h->walls_xz = d->ip || d->kp;
+    for (int n = 0; n < nl; ++n) {  // walled x / z: ghosts from their relations, no images
+        h->L[n].g.px = d->ip ? 0 : 1;
+        h->L[n].g.pz = d->kp ? 0 : 1;
+    }
     for (int n = 0; n < nl; ++n) {
         LevelData& L = h->L[n];
         if (L.sx == L.sy && L.sy == L.sz) {  // mul_met's t/pot and the flux factor ppot2
@@ -1201,7 +1250,7 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     {
         const LevelData& C = h->L[nl - 1];
         const int n = C.g.nx * C.g.nz * (C.g.ny + 2);
-        if (n <= kDenseMax) {
+        if (n <= kDenseMax && !h->walls_xz) {  // the dense system assumes periodic x and z
             rc = mixed ? build_coarse_inverse<float>(h, nl, C.cf) : build_coarse_inverse<double>(h, nl, C.cd);
             if (rc) return rc;
             smem_max = std::max(smem_max, (size_t)n * (mixed ? 4 : 8));
@@ -1211,7 +1260,8 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     if ((rc = mixed ? set_smem_attrs<float>(h, smem_max) : set_smem_attrs<double>(h, smem_max))) return rc;
     const Geom& g = h->L[0].g;
     if ((rc = dalloc(h, (void**)&h->x, 8 * (size_t)g.n)) || (rc = dalloc(h, (void**)&h->b, 8 * (size_t)g.n)) ||
-        (rc = dalloc(h, (void**)&h->wbuf, 8 * 2 * (size_t)g.nx * g.nz)))
+        (rc = dalloc(h, (void**)&h->wbuf, 8 * 2 * (size_t)g.nx * g.nz)) ||
+        (h->walls_xz && (rc = dalloc(h, &h->sbuf, 8 * (size_t)side_cells(g)))))
         return rc;
     dim3 rg = red_grid(g);
     h->npart = (long long)rg.x * rg.y * rg.z;
@@ -1239,6 +1289,8 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         int p = (int)std::ceil(std::log(1e-10) / std::log(q));
         h->wall_passes = p < 2 ? 2 : (p > 40 ? 40 : p);
     }
+    // walled x / z: their ghosts and edges couple to the y-wall rows
+    if (h->walls_xz) h->wall_passes = std::max(h->wall_passes, 30);
     return PLES_MG_OK;
 }
 
@@ -1249,7 +1301,8 @@ int upload_cs(ples_mg_handle* h, const double* const cs[6], bool device_ptrs) {
     for (int s = 0; s < 6; ++s) {
         const double* src = cs ? cs[s] : nullptr;
         if (!src) { h->cs_c[s] = nullptr; continue; }
-        if (s != 2 && s != 3) { h->cs_c[s] = nullptr; continue; }  // periodic x/z: unused
+        // fluxes of periodic directions are unused
+        if ((s < 2 && !h->d.ip) || (s > 3 && !h->d.kp)) { h->cs_c[s] = nullptr; continue; }
         // persistent per-handle buffers, allocated on first use
         if (!h->cs_buf[s]) {
             void* buf = nullptr;
@@ -1553,16 +1606,14 @@ int ples_mg_apply_ghost_fill(ples_mg_handle* h, int level, double* pr, const dou
             free_tmp(tmp);
             return rc;
         }
-        const double* c3 = nullptr;
-        const double* c4 = nullptr;
+        const double* const* csd = nullptr;
         if (level == 1 && cs) {
             if ((rc = upload_cs(h, cs, false))) { free_tmp(tmp); return rc; }
-            c3 = h->cs_c[2];
-            c4 = h->cs_c[3];
+            csd = h->cs_c;
         }
-        // the handle's wall buffer is sized for level 1 and serves every level
+        // the handle's wall buffers are sized for level 1 and serve every level
         ghost_xz<double>(h, g, P);
-        wall_fill(h, P, c3, c4, level == 1 ? 1.0 / h->d.dt : 0.0, passes, g, c);
+        wall_fill(h, P, csd, level == 1 ? 1.0 / h->d.dt : 0.0, passes, g, c);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) { free_tmp(tmp); return fail(h, PLES_MG_CUDA_ERROR, "ghost fill: %s", cudaGetErrorString(e)); }
         rc = get_box(h, g, 1, P, pr, tmp);
@@ -1864,6 +1915,7 @@ int ples_mg_project(ples_mg_handle* h, double* uc, double* vc, double* wc, doubl
                     double* fi, double rel_tol, int max_cycles, ples_mg_stats* stats) {
     if (!h || !uc || !vc || !wc || !fi || max_cycles < 0 || ((u || v || w) && !(u && v && w)))
         return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    if (h->walls_xz) return fail(h, PLES_MG_BAD_ARG, "the projection step needs periodic x and z (ip = kp = 0)");
     return with_device(h, [&]() -> int {
         return project_core(h, uc, vc, wc, u, v, w, fi, rel_tol, max_cycles, stats, false);
     });
@@ -1891,6 +1943,7 @@ int ples_mg_step(ples_mg_handle* h, double* u, double* v, double* w, double* uc,
                  double rel_tol, int max_cycles, ples_mg_stats* stats) {
     if (!h || !u || !v || !w || !uc || !vc || !wc || !fi || max_cycles < 0)
         return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    if (h->walls_xz) return fail(h, PLES_MG_BAD_ARG, "the pressure step needs periodic x and z (ip = kp = 0)");
     return with_device(h, [&]() -> int {
         return project_core(h, uc, vc, wc, u, v, w, fi, rel_tol, max_cycles, stats, true);
     });

@@ -55,7 +55,7 @@ def _desc(**kw):
     return d, keep
 
 
-@pytest.mark.parametrize("field,value", [("jp", 0), ("ip", 1), ("kp", 1), ("jx", 4), ("precision", 7),
+@pytest.mark.parametrize("field,value", [("jp", 0), ("ip", 2), ("kp", -1), ("jx", 4), ("precision", 7),
                                          ("coords_layout", 5), ("dt", 0.0), ("smoother", 3), ("jz", 15)])
 def test_bad_descriptor_rejected_without_device(field, value):
     lib = mg.load()

@@ -1,0 +1,122 @@
+"""Walls in x and z (ip = 1, kp = 1) against the oracle.
+
+With walls the ghost cells of that direction hold the value of the wall
+relation of mul_boun_sndrcv (multigrid.f03:1111-1158, 1280-1316: the flux
+through the wall face equals an*cs/dt) and its edge copies (:1360-1742),
+instead of periodic images.  The oracle runs two emulated ranks where z has
+walls: on one rank the reference leaves the edge cells of the last plane
+unset (multigrid.f03:1628-1742 uses else-if on the rank), so its fixed point
+depends on stale values there.
+
+Tolerances: face metric bit-exact; ghost layer at the fixed point of the
+fill within 1e-12; solves to ||r||/||b|| <= 1e-10 within 1e-8 of the oracle's
+converged solution (zero mean, L2 and max).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from ples_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+DIMS = (32, 16, 32)
+CASES = [(1, 0, 1), (0, 1, 2), (1, 1, 2)]  # ip, kp, oracle ranks
+
+
+def _zm(fi):
+    p = fi[1:-1, 1:-1, 1:-1]
+    return p - p.mean()
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b), np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.fixture(scope="module")
+def grid():
+    return S.wavy_channel_grid(*DIMS, 0.08, 2.0)
+
+
+@pytest.mark.parametrize("ip,kp,nproc", CASES)
+def test_metric_with_walls_bit_exact(grid, ip, kp, nproc):
+    from ples_gb300 import mg
+    x, y, z = grid
+    orc = Oracle(x, y, z, ip=ip, kp=kp, islor=1, nproc=nproc)
+    with mg.Multigrid(x, y, z, ip=ip, kp=kp, nlevmax=4) as m:
+        for level in (1, 2, 3):
+            for name in mg.METRIC_NAMES:
+                a, b = m.metric(level, name), orc.metric(level, name)
+                assert np.array_equal(a, b), (level, name, np.abs(a - b).max())
+
+
+def test_wall_ghost_fill_fixed_point(grid):
+    """x walls (the oracle's ghost fill runs on one rank; with z walls its
+    last-plane edges need the two-rank emulation, covered by the solves)."""
+    from ples_gb300 import mg
+    x, y, z = grid
+    jx, jy, jz = DIMS
+    ip, kp = 1, 0
+    orc = Oracle(x, y, z, ip=ip, kp=kp, islor=1, dt=0.5)
+    rng = np.random.default_rng(5)
+    shapes = ((jy, jz), (jy, jz), (jx, jz), (jx, jz), (jx, jy), (jx, jy))
+    cs = [np.asfortranarray(0.3 * rng.standard_normal(s)) for s in shapes]
+    with mg.Multigrid(x, y, z, ip=ip, kp=kp, nlevmax=4, dt=0.5) as m:
+        for level in (1, 2):
+            nx, ny, nz = orc.dims(level)
+            pr = np.asfortranarray(rng.standard_normal((nx + 2, ny + 2, nz + 2)))
+            ref = pr.copy(order="F")
+            for _ in range(40):
+                ref = orc.ghost_fill(level, ref, cs=cs)
+            out = m.ghost_fill(level, pr, cs=cs, passes=200)
+            np.testing.assert_array_equal(out[1:-1, 1:-1, 1:-1], pr[1:-1, 1:-1, 1:-1])
+            assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max(), (level, np.abs(out - ref).max())
+
+
+@pytest.mark.parametrize("ip,kp,nproc", CASES)
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solve_with_walls_matches_oracle(grid, ip, kp, nproc, precision):
+    from ples_gb300 import mg
+    x, y, z = grid
+    rhs = S.divergence_rhs(*DIMS, seed=4)
+    fo, *_ = Oracle(x, y, z, ip=ip, kp=kp, islor=1, nproc=nproc).multi(rhs, eps=1e-13, ficycle=600)
+    with mg.Multigrid(x, y, z, ip=ip, kp=kp, precision=precision) as m:
+        fi, st = m.solve(rhs, rel_tol=1e-10)
+    assert st["status"] == mg.OK and st["rel_residual"] <= 1e-10
+    l2, mx = _rel(_zm(fi), _zm(fo))
+    assert l2 <= 1e-8 and mx <= 1e-8, (l2, mx)
+
+
+def test_wall_fluxes_on_x_and_z_walls(grid):
+    """cs1, cs2 (x walls) and cs5, cs6 (z walls) at dt = 0.5 with the
+    right-hand side made compatible with their net flux."""
+    from ples_gb300 import mg
+    x, y, z = grid
+    jx, jy, jz = DIMS
+    dt = 0.5
+    rng = np.random.default_rng(12)
+    cs = [np.asfortranarray(0.1 * rng.standard_normal(s))
+          for s in ((jy, jz), (jy, jz), (jx, jz), (jx, jz), (jx, jy), (jx, jy))]
+    net = ((cs[1].sum() - cs[0].sum()) + (cs[3].sum() - cs[2].sum()) + (cs[5].sum() - cs[4].sum())) / dt
+    rhs = S.divergence_rhs(*DIMS, seed=8, dt=dt)
+    rhs = rhs + net / rhs.size
+    orc = Oracle(x, y, z, ip=1, kp=1, islor=1, nproc=2, dt=dt)
+    fo, *_ = orc.multi(rhs, cs=cs, eps=1e-13, ficycle=600)
+    with mg.Multigrid(x, y, z, ip=1, kp=1, dt=dt) as m:
+        fi, st = m.solve(rhs, cs=cs, rel_tol=1e-10)
+    assert st["status"] == mg.OK and abs(st["rhs_mean_removed"]) < 1e-12
+    l2, mx = _rel(_zm(fi), _zm(fo))
+    assert l2 <= 1e-8 and mx <= 1e-8, (l2, mx)
+
+
+def test_walls_rejected_where_unsupported(grid):
+    from ples_gb300 import mg
+    x, y, z = grid
+    with mg.Multigrid(x, y, z, ip=1) as m:
+        with pytest.raises(mg.PlesMGError):
+            mg.Batch([m])
+        jx, jy, jz = DIMS
+        with pytest.raises(mg.PlesMGError):
+            m.project(np.zeros((jx + 1, jy, jz)), np.zeros((jx, jy + 1, jz)), np.zeros((jx, jy, jz + 1)),
+                      np.zeros((jx + 2, jy + 2, jz + 2)))
+    with pytest.raises(mg.PlesMGError):
+        mg.Multigrid(x, y, z, kp=1, solid=np.zeros(DIMS, dtype=bool))
