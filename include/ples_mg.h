@@ -181,8 +181,10 @@ int ples_mg_project(ples_mg_handle *h, double *uc, double *vc, double *wc, doubl
                     double *v, double *w, double *fi, double rel_tol, int max_cycles,
                     ples_mg_stats *stats);
 
-/* The whole pressure step: contra (fsrc/contra.f03:91-219, ip = kp = 0,
- * jp = 1, potenziale = 0) and then the projection above.  On entry u,v,w are
+/* The whole pressure step: contra (fsrc/contra.f03:31-219, jp = 1,
+ * potenziale = 0; with x / z walls their faces also take the wall velocity
+ * and give cs1/cs2, cs5/cs6, as on several ranks) and then the projection
+ * above (wall faces keep their flux).  On entry u,v,w are
  * the intermediate Cartesian velocities with their ghost cells (the wall
  * velocity in j = 0 and jy+1, periodic images in x and z) and uc,vc,wc the
  * previous contravariant ones, of which only the wall faces vc(:,0,:),

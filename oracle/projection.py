@@ -108,7 +108,17 @@ def face_normals(orc):
 def contra(orc, u, v, w, vc_old):
     """Returns (uc, vc, wc, cs3, cs4) from the cell-centred u, v, w
     (jx+2, jy+2, jz+2) and the previous vc, whose wall faces give the old
-    wall fluxes; cs3, cs4 are (jx, jz)."""
+    wall fluxes; cs3, cs4 are (jx, jz).  Periodic x and z."""
+    uc, vc, wc, cs = contra_walls(orc, u, v, w, None, vc_old, None)
+    return uc, vc, wc, cs[2], cs[3]
+
+
+def contra_walls(orc, u, v, w, uc_old, vc_old, wc_old):
+    """contra with the grid's periodicity (orc.ip, orc.kp): the faces of a
+    walled direction take the wall velocity of the ghost cell and give
+    cs = new minus old wall flux (contra.f03:34-67 x walls, 160-190 z walls,
+    several-rank form).  Returns (uc, vc, wc, [cs1..cs6]) with zero arrays
+    for periodic directions."""
     jx, jy, jz = orc.jx, orc.jy, orc.jz
     (csx, csy, csz, _), (etx, ety, etz, _), (ztx, zty, ztz, _) = face_normals(orc)
 
@@ -121,15 +131,27 @@ def contra(orc, u, v, w, vc_old):
     sj0, sj1 = np.s_[1:jx + 1, 1:jy, 1:jz + 1], np.s_[1:jx + 1, 2:jy + 1, 1:jz + 1]
     vc[:, 1:jy] = (avg(u, sj0, sj1) * etx[:, 1:jy] + avg(v, sj0, sj1) * ety[:, 1:jy]
                    + avg(w, sj0, sj1) * etz[:, 1:jy])
-    cs = []
-    for jf, jw in ((0, 0), (jy, jy + 1)):
+    cs = [np.zeros((jy, jz)), np.zeros((jy, jz)), None, None, np.zeros((jx, jy)), np.zeros((jx, jy))]
+    for s, (jf, jw) in enumerate(((0, 0), (jy, jy + 1))):
         flux = (u[1:jx + 1, jw, 1:jz + 1] * etx[:, jf] + v[1:jx + 1, jw, 1:jz + 1] * ety[:, jf]
                 + w[1:jx + 1, jw, 1:jz + 1] * etz[:, jf])
-        cs.append(flux - vc_old[:, jf])
+        cs[2 + s] = flux - vc_old[:, jf]
         vc[:, jf] = flux
+    if orc.ip == 1:
+        for s, (iff, iw) in enumerate(((0, 0), (jx, jx + 1))):
+            flux = (u[iw, 1:jy + 1, 1:jz + 1] * csx[iff] + v[iw, 1:jy + 1, 1:jz + 1] * csy[iff]
+                    + w[iw, 1:jy + 1, 1:jz + 1] * csz[iff])
+            cs[s] = flux - uc_old[iff]
+            uc[iff] = flux
     sk0, sk1 = np.s_[1:jx + 1, 1:jy + 1, 0:jz + 1], np.s_[1:jx + 1, 1:jy + 1, 1:jz + 2]
     wc = avg(u, sk0, sk1) * ztx + avg(v, sk0, sk1) * zty + avg(w, sk0, sk1) * ztz
-    return uc, vc, wc, cs[0], cs[1]
+    if orc.kp == 1:
+        for s, (kf, kw) in enumerate(((0, 0), (jz, jz + 1))):
+            flux = (u[1:jx + 1, 1:jy + 1, kw] * ztx[:, :, kf] + v[1:jx + 1, 1:jy + 1, kw] * zty[:, :, kf]
+                    + w[1:jx + 1, 1:jy + 1, kw] * ztz[:, :, kf])
+            cs[4 + s] = flux - wc_old[:, :, kf]
+            wc[:, :, kf] = flux
+    return uc, vc, wc, cs
 
 
 def diver(uc, vc, wc, dt):
@@ -160,10 +182,15 @@ def project(orc, fi, uc, vc, wc, u, v, w, dt):
     cg3 = (g["g33"] * (p(0, 0, 1, *b) - p(0, 0, 0, *b))
            + .25 * g["g31"] * (p(1, 0, 1, *b) + p(1, 0, 0, *b) - p(-1, 0, 1, *b) - p(-1, 0, 0, *b))
            + .25 * g["g32"] * (p(0, 1, 1, *b) + p(0, 1, 0, *b) - p(0, -1, 1, *b) - p(0, -1, 0, *b)))
-    uc2 = uc - dt * cg1
+    # wall faces keep their flux (vel_up.f03:188-285)
+    i0, i1 = (0, jx + 1) if orc.ip == 0 else (1, jx)
+    k0, k1 = (0, jz + 1) if orc.kp == 0 else (1, jz)
+    uc2 = uc.copy()
+    uc2[i0:i1] -= dt * cg1[i0:i1]
     vc2 = vc.copy()
     vc2[:, 1:jy] -= dt * cg2[:, 1:jy]
-    wc2 = wc - dt * cg3
+    wc2 = wc.copy()
+    wc2[:, :, k0:k1] -= dt * cg3[:, :, k0:k1]
     out = [uc2, vc2, wc2]
     if u is not None:
         (csx, csy, csz, _), (etx, ety, etz, _), (ztx, zty, ztz, _) = face_normals(orc)
@@ -178,10 +205,12 @@ def project(orc, fi, uc, vc, wc, u, v, w, dt):
                          - zt[:, :, :-1] * sb)
             a2 = a.copy()
             a2[1:-1, 1:-1, 1:-1] += gr
-            a2[0, 1:-1, 1:-1] = a2[jx, 1:-1, 1:-1]
-            a2[jx + 1, 1:-1, 1:-1] = a2[1, 1:-1, 1:-1]
-            a2[:, 1:-1, 0] = a2[:, 1:-1, jz]
-            a2[:, 1:-1, jz + 1] = a2[:, 1:-1, 1]
+            if orc.ip == 0:  # periodic images (vel_up.f03:82-100)
+                a2[0, 1:-1, 1:-1] = a2[jx, 1:-1, 1:-1]
+                a2[jx + 1, 1:-1, 1:-1] = a2[1, 1:-1, 1:-1]
+            if orc.kp == 0:
+                a2[:, 1:-1, 0] = a2[:, 1:-1, jz]
+                a2[:, 1:-1, jz + 1] = a2[:, 1:-1, 1]
             res.append(a2)
         out += res
     return out

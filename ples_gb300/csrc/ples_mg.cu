@@ -1743,9 +1743,10 @@ __global__ void k_project_faces(Geom g, Coef<double> c, const double* __restrict
     const int k = blockIdx.z;
     if (i > g.nx || j > g.ny || k > g.nz) return;
     const long long q = g.at(i, j, k);
-    if (j >= 1 && k >= 1) uc[iuc(g, i, j, k)] -= dt * flux_x(g, c, x, q);
+    // wall faces keep their flux (vel_up.f03:188-285: i = ip..jx-ip, j = jp..jy-jp, k = kp..jz-kp)
+    if (j >= 1 && k >= 1 && (g.px || (i >= 1 && i <= g.nx - 1))) uc[iuc(g, i, j, k)] -= dt * flux_x(g, c, x, q);
     if (i >= 1 && k >= 1 && j >= 1 && j <= g.ny - 1) vc[ivc(g, i, j, k)] -= dt * flux_y(g, c, x, q);
-    if (i >= 1 && j >= 1) wc[iwc(g, i, j, k)] -= dt * flux_z(g, c, x, q);
+    if (i >= 1 && j >= 1 && (g.pz || (k >= 1 && k <= g.nz - 1))) wc[iwc(g, i, j, k)] -= dt * flux_z(g, c, x, q);
 }
 
 // Cartesian pressure gradient at the cell centres times -dt/2 J^-1
@@ -1773,8 +1774,8 @@ __global__ void k_project_cells(Geom g, const double* __restrict__ x, Normals nr
         gr[d] = coef * (cs[q] * se - cs[q - 1] * sw + et[q] * sn - et[q - sj] * ss + zt[q] * sf - zt[q - sk] * sb);
     }
     double* vel[3] = {u, v, w};
-    const int gi = i == g.nx ? 0 : (i == 1 ? g.nx + 1 : -1);
-    const int gk = k == g.nz ? 0 : (k == 1 ? g.nz + 1 : -1);
+    const int gi = !g.px ? -1 : (i == g.nx ? 0 : (i == 1 ? g.nx + 1 : -1));  // images in periodic directions
+    const int gk = !g.pz ? -1 : (k == g.nz ? 0 : (k == 1 ? g.nz + 1 : -1));
     for (int d = 0; d < 3; ++d) {
         double* a = vel[d];
         const double nv = a[icell(g, i, j, k)] + gr[d];
@@ -1786,13 +1787,19 @@ __global__ void k_project_cells(Geom g, const double* __restrict__ x, Normals nr
 }
 
 // intermediate contravariant velocities from the Cartesian ones and the
-// wall fluxes cs3/cs4 (contra.f03:31-200 with ip = kp = 0, jp = 1,
-// potenziale = 0): interior faces get the face-normal projection of the
-// average of their two cells; the wall faces get that of the wall velocity
-// (the ghost cell), and cs = new wall flux - old wall flux
+// wall fluxes (contra.f03:31-219, jp = 1, potenziale = 0): interior faces get
+// the face-normal projection of the average of their two cells; a wall face
+// gets that of the wall velocity (the ghost cell), and cs = new wall flux -
+// old wall flux.  z walls follow the reference's several-rank form (both
+// wall faces set, cs5 and cs6).
+struct WallFlux {
+    double* cs[6];  // cs1..cs6, null for periodic directions
+};
 __global__ void k_contra(Geom g, Normals nrm, const double* __restrict__ u, const double* __restrict__ v,
                          const double* __restrict__ w, double* __restrict__ uc, double* __restrict__ vc,
-                         double* __restrict__ wc, double* __restrict__ cs3, double* __restrict__ cs4) {
+                         double* __restrict__ wc, WallFlux wf) {
+    double* cs3 = wf.cs[2];
+    double* cs4 = wf.cs[3];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -1800,9 +1807,18 @@ __global__ void k_contra(Geom g, Normals nrm, const double* __restrict__ u, cons
     const long long q = g.at(i, j, k);
     auto C = [&](const double* a, int ii, int jj, int kk) { return a[icell(g, ii, jj, kk)]; };
     if (j >= 1 && k >= 1) {  // csi face i = 0..jx
-        const double ui = .5 * (C(u, i, j, k) + C(u, i + 1, j, k)), vi = .5 * (C(v, i, j, k) + C(v, i + 1, j, k)),
-                     wi = .5 * (C(w, i, j, k) + C(w, i + 1, j, k));
-        uc[iuc(g, i, j, k)] = ui * nrm.p[0][q] + vi * nrm.p[1][q] + wi * nrm.p[2][q];
+        const long long qu = iuc(g, i, j, k);
+        if (g.px || (i >= 1 && i <= g.nx - 1)) {
+            const double ui = .5 * (C(u, i, j, k) + C(u, i + 1, j, k)), vi = .5 * (C(v, i, j, k) + C(v, i + 1, j, k)),
+                         wi = .5 * (C(w, i, j, k) + C(w, i + 1, j, k));
+            uc[qu] = ui * nrm.p[0][q] + vi * nrm.p[1][q] + wi * nrm.p[2][q];
+        } else {  // x wall: the wall velocity in the ghost column
+            const int iw = i == 0 ? 0 : g.nx + 1;
+            const double flux = C(u, iw, j, k) * nrm.p[0][q] + C(v, iw, j, k) * nrm.p[1][q] + C(w, iw, j, k) * nrm.p[2][q];
+            double* cs = i == 0 ? wf.cs[0] : wf.cs[1];
+            cs[(long long)(k - 1) * g.ny + (j - 1)] = flux - uc[qu];
+            uc[qu] = flux;
+        }
     }
     if (i >= 1 && k >= 1) {  // eta face j = 0..jy
         const long long qv = ivc(g, i, j, k);
@@ -1819,9 +1835,18 @@ __global__ void k_contra(Geom g, Normals nrm, const double* __restrict__ u, cons
         }
     }
     if (i >= 1 && j >= 1) {  // zeta face k = 0..jz
-        const double ui = .5 * (C(u, i, j, k) + C(u, i, j, k + 1)), vi = .5 * (C(v, i, j, k) + C(v, i, j, k + 1)),
-                     wi = .5 * (C(w, i, j, k) + C(w, i, j, k + 1));
-        wc[iwc(g, i, j, k)] = ui * nrm.p[6][q] + vi * nrm.p[7][q] + wi * nrm.p[8][q];
+        const long long qw = iwc(g, i, j, k);
+        if (g.pz || (k >= 1 && k <= g.nz - 1)) {
+            const double ui = .5 * (C(u, i, j, k) + C(u, i, j, k + 1)), vi = .5 * (C(v, i, j, k) + C(v, i, j, k + 1)),
+                         wi = .5 * (C(w, i, j, k) + C(w, i, j, k + 1));
+            wc[qw] = ui * nrm.p[6][q] + vi * nrm.p[7][q] + wi * nrm.p[8][q];
+        } else {  // z wall: the wall velocity in the ghost plane
+            const int kw = k == 0 ? 0 : g.nz + 1;
+            const double flux = C(u, i, j, kw) * nrm.p[6][q] + C(v, i, j, kw) * nrm.p[7][q] + C(w, i, j, kw) * nrm.p[8][q];
+            double* cs = k == 0 ? wf.cs[4] : wf.cs[5];
+            cs[(long long)(j - 1) * g.nx + (i - 1)] = flux - wc[qw];
+            wc[qw] = flux;
+        }
     }
 }
 
@@ -1866,12 +1891,19 @@ int project_core(ples_mg_handle* h, double* uc, double* vc, double* wc, double* 
     k_compact_to_box<<<compact_grid(g, 1), dim3(32, 4), 0, h->st>>>(g, 1, h->fi_c, h->x);
     ++h->launches;
     if (with_contra) {
-        for (int s = 2; s <= 3; ++s)
-            if (!h->cs_buf[s] && (rc = dalloc(h, (void**)&h->cs_buf[s], 8 * (size_t)g.nx * g.nz))) return rc;
+        // wall fluxes of the directions with walls: y always, x / z when walled
+        const size_t ncs[6] = {(size_t)g.ny * g.nz, (size_t)g.ny * g.nz, (size_t)g.nx * g.nz,
+                               (size_t)g.nx * g.nz, (size_t)g.nx * g.ny, (size_t)g.nx * g.ny};
+        const bool used[6] = {!g.px, !g.px, true, true, !g.pz, !g.pz};
+        WallFlux wf;
+        for (int s = 0; s < 6; ++s) {
+            if (used[s] && !h->cs_buf[s] && (rc = dalloc(h, (void**)&h->cs_buf[s], 8 * ncs[s]))) return rc;
+            wf.cs[s] = used[s] ? h->cs_buf[s] : nullptr;
+            h->cs_c[s] = wf.cs[s];
+        }
         k_contra<<<dim3((g.nx + 1 + 31) / 32, (g.ny + 1 + 3) / 4, g.nz + 1), dim3(32, 4), 0, h->st>>>(
-            g, pn, h->d_u, h->d_v, h->d_w, h->d_uc, h->d_vc, h->d_wc, h->cs_buf[2], h->cs_buf[3]);
+            g, pn, h->d_u, h->d_v, h->d_w, h->d_uc, h->d_vc, h->d_wc, wf);
         ++h->launches;
-        for (int s = 0; s < 6; ++s) h->cs_c[s] = (s == 2 || s == 3) ? h->cs_buf[s] : nullptr;
     } else if ((rc = upload_cs(h, nullptr, false))) {
         return rc;
     }
@@ -1915,7 +1947,6 @@ int ples_mg_project(ples_mg_handle* h, double* uc, double* vc, double* wc, doubl
                     double* fi, double rel_tol, int max_cycles, ples_mg_stats* stats) {
     if (!h || !uc || !vc || !wc || !fi || max_cycles < 0 || ((u || v || w) && !(u && v && w)))
         return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
-    if (h->walls_xz) return fail(h, PLES_MG_BAD_ARG, "the projection step needs periodic x and z (ip = kp = 0)");
     return with_device(h, [&]() -> int {
         return project_core(h, uc, vc, wc, u, v, w, fi, rel_tol, max_cycles, stats, false);
     });
@@ -1943,7 +1974,6 @@ int ples_mg_step(ples_mg_handle* h, double* u, double* v, double* w, double* uc,
                  double rel_tol, int max_cycles, ples_mg_stats* stats) {
     if (!h || !u || !v || !w || !uc || !vc || !wc || !fi || max_cycles < 0)
         return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
-    if (h->walls_xz) return fail(h, PLES_MG_BAD_ARG, "the pressure step needs periodic x and z (ip = kp = 0)");
     return with_device(h, [&]() -> int {
         return project_core(h, uc, vc, wc, u, v, w, fi, rel_tol, max_cycles, stats, true);
     });

@@ -114,9 +114,65 @@ def test_walls_rejected_where_unsupported(grid):
     with mg.Multigrid(x, y, z, ip=1) as m:
         with pytest.raises(mg.PlesMGError):
             mg.Batch([m])
-        jx, jy, jz = DIMS
-        with pytest.raises(mg.PlesMGError):
-            m.project(np.zeros((jx + 1, jy, jz)), np.zeros((jx, jy + 1, jz)), np.zeros((jx, jy, jz + 1)),
-                      np.zeros((jx + 2, jy + 2, jz + 2)))
     with pytest.raises(mg.PlesMGError):
         mg.Multigrid(x, y, z, kp=1, solid=np.zeros(DIMS, dtype=bool))
+
+
+def _step_inputs_walls(ip, kp, seed):
+    """Intermediate Cartesian velocities with wall velocities in the ghost
+    cells of walled directions and images in periodic ones; previous
+    contravariant velocities whose wall faces carry mean-zero old fluxes."""
+    jx, jy, jz = DIMS
+    rng = np.random.default_rng(seed)
+    u, v, w = (rng.standard_normal((jx + 2, jy + 2, jz + 2)) for _ in range(3))
+    for a in (u, v, w):
+        if ip == 0:
+            a[0], a[jx + 1] = a[jx], a[1]
+        if kp == 0:
+            a[:, :, 0], a[:, :, jz + 1] = a[:, :, jz], a[:, :, 1]
+    uc = rng.standard_normal((jx + 1, jy, jz))
+    vc = rng.standard_normal((jx, jy + 1, jz))
+    wc = rng.standard_normal((jx, jy, jz + 1))
+    for f in (0, jy):
+        vc[:, f] -= vc[:, f].mean()
+    if ip:
+        for f in (0, jx):
+            uc[f] -= uc[f].mean()
+    if kp:
+        for f in (0, jz):
+            wc[:, :, f] -= wc[:, :, f].mean()
+    return u, v, w, uc, vc, wc
+
+
+@pytest.mark.parametrize("ip,kp,nproc", CASES)
+def test_pressure_step_with_walls_matches_oracle(grid, ip, kp, nproc):
+    """ples_mg_step with x/z walls: contra's wall fluxes cs1/cs2/cs5/cs6 on
+    the device, the solve, and vel_up leaving the wall faces alone, against
+    the oracle chain (to 1e-8 for the pressure, 1e-12 for the velocities);
+    the result is divergence free against the old wall fluxes."""
+    from oracle.projection import contra_walls, diver, project
+    from ples_gb300 import mg
+    x, y, z = grid
+    jx, jy, jz = DIMS
+    dt = 0.01
+    u, v, w, uc, vc, wc = _step_inputs_walls(ip, kp, 50 + ip + 2 * kp)
+    orc = Oracle(x, y, z, ip=ip, kp=kp, islor=1, dt=dt, nproc=nproc)
+    uc1, vc1, wc1, cs = contra_walls(orc, u, v, w, uc, vc, wc)
+    with mg.Multigrid(x, y, z, ip=ip, kp=kp, dt=dt) as m:
+        (u2, v2, w2, uc2, vc2, wc2, fi), st = m.step(u, v, w, uc, vc, wc, np.zeros((jx + 2, jy + 2, jz + 2)),
+                                                     rel_tol=1e-10)
+    assert st["status"] == mg.OK and abs(st["rhs_mean_removed"]) < 1e-9
+    ref, *_ = orc.multi(diver(uc1, vc1, wc1, dt), cs=cs, eps=1e-13, ficycle=800)
+    l2, mx = _rel(_zm(fi), _zm(ref))
+    assert l2 <= 1e-8 and mx <= 1e-8, (l2, mx)
+    exp = project(orc, fi, uc1, vc1, wc1, u, v, w, dt)
+    for got, want in zip((uc2, vc2, wc2, u2, v2, w2), exp):
+        assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    old = [uc2.copy(), vc2.copy(), wc2.copy()]
+    old[1][:, 0], old[1][:, jy] = vc[:, 0], vc[:, jy]
+    if ip:
+        old[0][0], old[0][jx] = uc[0], uc[jx]
+    if kp:
+        old[2][:, :, 0], old[2][:, :, jz] = wc[:, :, 0], wc[:, :, jz]
+    d0 = np.abs(diver(uc1, vc1, wc1, 1.0)).max()
+    assert np.abs(diver(*old, 1.0)).max() <= 1e-8 * d0
