@@ -327,7 +327,10 @@ __global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp) {
     for (int j = 1; j <= g.ny; ++j) {
         const long long q = g.at(i, j, k);
         const T a = ld(c.a2, q - g.sj), cc = ld(c.a2, q);
-        const T b = -(cc + a + ld(c.a1, q) + ld(c.a1, q - 1) + ld(c.a3, q) + ld(c.a3, q - g.sk));
+        // the faces of x / z walls carry no flux in the relaxed equation
+        const T ae = !g.px && i == g.nx ? T(0) : ld(c.a1, q), aw = !g.px && i == 1 ? T(0) : ld(c.a1, q - 1);
+        const T af = !g.pz && k == g.nz ? T(0) : ld(c.a3, q), ab = !g.pz && k == 1 ? T(0) : ld(c.a3, q - g.sk);
+        const T b = -(cc + a + ae + aw + af + ab);
         prev = b == T(0) ? T(0) : cc / (b - a * prev);
         cp[q] = prev;
     }
@@ -420,7 +423,11 @@ __device__ __forceinline__ T from_east(T v, T h) {
 // holds its pressure column; the rows and the arithmetic of each equation
 // are those of the strided form (same expressions, same order).
 // Loads ahead: rows PLES_LINE_PF_ROWS further on are hinted into L2.
-template <typename T, bool ZEBRA, bool ZIN>
+// WALLS: x / z walls; as in the reference's line SOR (multigrid.f03:2120-
+// 2160, masks i_dx..i_in of sett.f03) a wall face carries no flux in the
+// relaxed equation (the correction's wall flux is zero), while the ghost
+// cells beyond it still enter the cross terms of the other faces.
+template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false>
 __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, const T* __restrict__ cpa,
                                            const T* __restrict__ pin, const T* __restrict__ pk,
                                            const T* __restrict__ rh, T omega, int zk, int i, int k, bool odd, T* G,
@@ -546,9 +553,15 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
                 if (a2s == T(0)) { im = T(1); f = T(0); tp = P0; }  // wall row below a solid cell
             }
         } else {
-            const T a1w = from_west(a1e, a1h), b12w = from_west(b12v, b12h), b13w = from_west(b13v, b13h);
+            T a1w = from_west(a1e, a1h), b12w = from_west(b12v, b12h), b13w = from_west(b13v, b13h);
             const T pef = from_east(F0, hF0), pwf = from_west(F0, hF0);
             const T peb = from_east(B0, hB0), pwb = from_west(B0, hB0);
+            if (WALLS) {  // after the shuffles: the neighbours keep their own faces
+                if (!g.px && i == 1) a1w = b12w = b13w = T(0);
+                if (!g.px && i == g.nx) a1e = b12v = b13v = T(0);
+                if (!g.pz && k == 1) a3b = b31b = b32b = T(0);
+                if (!g.pz && k == g.nz) a3f = b31v = b32v = T(0);
+            }
             if (act) {
                 a = a2s;
                 const T b = -(a2v + a + a1e + a1w + a3f + a3b);
@@ -600,7 +613,7 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
 // b12 for the odd lanes east of them (shuffled across), lane 0 the column
 // i0-1 outside the tile (its old pressure rows and the two coefficients),
 // and b21 of row j-1 is carried from the previous row.
-template <typename T, bool ZIN>
+template <typename T, bool ZIN, bool WALLS = false>
 __device__ __forceinline__ void odd_x_rows(const Geom& g, const Coef<T>& c, const T* __restrict__ cpa,
                                            const T* __restrict__ pin, T omega, T* G, T* CP, int i, int k) {
     constexpr int kXR = 2;
@@ -643,10 +656,17 @@ __device__ __forceinline__ void odd_x_rows(const Geom& g, const Coef<T>& c, cons
         for (int u = 0; u < kXR; ++u) {
             const int j = jb + u;
             if (j >= j1) break;
-            const T a1w = from_west(a1[u], a1h[u]);
-            const T b12w = from_west(b12[u], b12h[u]);
+            T a1w = from_west(a1[u], a1h[u]);
+            T b12w = from_west(b12[u], b12h[u]);
             const T b21s = u == 0 ? b21c : b21[u - 1];
             if (mine) {
+                T a1e = a1[u], b12e = b12[u], b31f = b31[u], b31k = b31b[u];
+                if (WALLS) {
+                    if (!g.px && i == 1) a1w = b12w = T(0);
+                    if (!g.px && i == g.nx) a1e = b12e = T(0);
+                    if (!g.pz && k == 1) b31k = T(0);
+                    if (!g.pz && k == g.nz) b31f = T(0);
+                }
                 const bool l0 = lane == 0;
                 const T pw = l0 ? wv[u + 1] : G[j * 32 + lane - 1];
                 const T pwn = j < nj - 1 ? (l0 ? wv[u + 2] : G[(j + 1) * 32 + lane - 1]) : T(0);
@@ -659,8 +679,8 @@ __device__ __forceinline__ void odd_x_rows(const Geom& g, const Coef<T>& c, cons
                     tx = b21s * (pe + EV(j - 1) - pw - pws);
                 } else {
                     const T pen = EV(j + 1), pes = EV(j - 1);
-                    tx = a1[u] * pe + a1w * pw + b12[u] * (pen - pes) - b12w * (pwn - pws) +
-                         b21[u] * (pen + pe - pwn - pw) - b21s * (pe + pes - pw - pws) + (b31[u] - b31b[u]) * (pe - pw);
+                    tx = a1e * pe + a1w * pw + b12e * (pen - pes) - b12w * (pwn - pws) +
+                         b21[u] * (pen + pe - pwn - pw) - b21s * (pe + pes - pw - pws) + (b31f - b31k) * (pe - pw);
                 }
                 const T im = CP[j * 32 + lane];
                 G[j * 32 + lane] -= omega * tx * im;
@@ -735,7 +755,7 @@ __device__ __forceinline__ void relax_store(const Geom& g, const T* __restrict__
 //         the first parity, = pout for the second); output to pout.
 // ZIN: pin is identically zero (first sweep of a correction); zk: pk is too.
 // Shared memory: 3 arrays [ny+2][32] and the segment maps [2][warps][32].
-template <typename T, bool ZEBRA, bool ZIN>
+template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false>
 __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
@@ -753,13 +773,13 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
     const int i = B.x * 32 + lane + 1;
     const bool act = i <= g.nx;
     const bool odd = ZEBRA && (i & 1);  // updated in the second half
-    build_rows<T, ZEBRA, ZIN>(g, c, cpa, pin, pk, rh, omega, zk, i, k, odd, G, AL, CP);
+    build_rows<T, ZEBRA, ZIN, WALLS>(g, c, cpa, pin, pk, rh, omega, zk, i, k, odd, G, AL, CP);
     T* SU = CP + nj * 32;  // segment maps of the parallel Thomas solve
     T* SV = SU + nw * 32;
     const int nhalf = ZEBRA ? 2 : 1;
     for (int half = 0; half < nhalf; ++half) {
         const bool mine = act && (!ZEBRA || ((i & 1) == half));
-        if (ZEBRA && half == 1) odd_x_rows<T, ZIN>(g, c, cpa, pin, omega, G, CP, i, k);
+        if (ZEBRA && half == 1) odd_x_rows<T, ZIN, WALLS>(g, c, cpa, pin, omega, G, CP, i, k);
         __syncthreads();
         seg_thomas(G, AL, CP, nj, mine, SU, SV);
         if (mine) store_rows(g, pout, G, i, k);
@@ -768,19 +788,19 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
 }
 // the same smoother with 16 warps per CTA (shorter row segments per warp,
 // for coarse levels whose few CTAs leave most SMs idle)
-template <typename T, bool ZEBRA, bool ZIN>
+template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false>
 __global__ void __launch_bounds__(512, sizeof(T) == 4 ? 2 : 1) k_line_relax_w(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
                                                     int kpar, int zk) {
-    k_line_relax_blk<T, ZEBRA, ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
+    k_line_relax_blk<T, ZEBRA, ZIN, WALLS>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
 }
-template <typename T, bool ZEBRA, bool ZIN>
+template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? PLES_LINE_MIN_BLOCKS : 2) k_line_relax(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
                                                     int kpar, int zk) {
-    k_line_relax_blk<T, ZEBRA, ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
+    k_line_relax_blk<T, ZEBRA, ZIN, WALLS>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
 }
 
 // ---------------------------------------------------------------------------

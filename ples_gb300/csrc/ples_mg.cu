@@ -132,6 +132,20 @@ template <typename T>
 __global__ void k_side_edges(Geom g, T* __restrict__ p, T* __restrict__ p2, int zero) {
     k_side_edges_blk<T>(g, p, p2, zero);
 }
+// the three steps in one CTA for a small level (its face ghosts in shared memory)
+constexpr int kSideSmall = 4096;
+template <typename T>
+__global__ void __launch_bounds__(1024) k_side_fill_small(Geom g, Coef<T> c, T* __restrict__ p, T* __restrict__ p2,
+                                                          int zero) {
+    __shared__ T w[kSideSmall];
+    const long long n = side_cells(g);
+    for (int b = 0; (long long)b * blockDim.x < n; ++b)
+        k_side_compute_blk<T>(g, c, p, w, nullptr, nullptr, nullptr, nullptr, 0.0, zero, Blk{b, 0, 0, 1, 1, 1});
+    __syncthreads();
+    for (int b = 0; (long long)b * blockDim.x < n; ++b) k_side_scatter_blk<T>(g, p, p2, w, Blk{b, 0, 0, 1, 1, 1});
+    __syncthreads();
+    k_side_edges_blk<T>(g, p, p2, zero);
+}
 
 // contraction factor of the Jacobi wall fill: max 2(|B21|+|B23|)/A2
 __global__ void k_wall_contraction(Geom g, Coef<double> c, unsigned long long* out) {
@@ -316,6 +330,13 @@ int set_smem_attrs(ples_mg_handle* h, size_t smem) {
     CK(cudaFuncSetAttribute(k_line_relax<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_w<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_w<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the forms for x / z walls
+    CK(cudaFuncSetAttribute(k_line_relax<T, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax<T, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_w<T, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_w<T, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_dense_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
 }
@@ -397,6 +418,11 @@ void side_fill(ples_mg_handle* h, const Geom& g, const Coef<T>& c, T* p, T* p2, 
                double an_dt, bool zero) {
     const long long n = side_cells(g);
     if (n == 0) return;
+    if (n <= kSideSmall && !cs) {  // one launch for a small level
+        k_side_fill_small<T><<<1, 1024, 0, h->st>>>(g, c, p, p2, zero ? 1 : 0);
+        ++h->launches;
+        return;
+    }
     const unsigned nb = (unsigned)((n + 255) / 256);
     k_side_compute<T><<<nb, 256, 0, h->st>>>(g, c, p, (T*)h->sbuf, cs ? cs[0] : nullptr, cs ? cs[1] : nullptr,
                                              cs ? cs[4] : nullptr, cs ? cs[5] : nullptr, an_dt, zero ? 1 : 0);
@@ -446,23 +472,25 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
         if (staged) {
         } else if (h->smoother != 1) {  // zebra: two launches, k parities
             dim3 grd((L.g.nx + 31) / 32, (L.g.nz + 1) / 2);
-            auto kern = nt > 256 ? (zin ? k_line_relax_w<T, true, true> : k_line_relax_w<T, true, false>)
-                                 : (zin ? k_line_relax<T, true, true> : k_line_relax<T, true, false>);
+            auto kern = walls ? (nt > 256 ? (zin ? k_line_relax_w<T, true, true, true> : k_line_relax_w<T, true, false, true>)
+                                          : (zin ? k_line_relax<T, true, true, true> : k_line_relax<T, true, false, true>))
+                              : (nt > 256 ? (zin ? k_line_relax_w<T, true, true> : k_line_relax_w<T, true, false>)
+                                          : (zin ? k_line_relax<T, true, true> : k_line_relax<T, true, false>));
             kern<<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
             kern<<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
             h->launches += 2;
         } else {  // Jacobi over lines
             dim3 grd((L.g.nx + 31) / 32, L.g.nz);
-            if (zin)
-                k_line_relax<T, false, true><<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 1);
-            else
-                k_line_relax<T, false, false><<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, 0);
+            auto kern = walls ? (zin ? k_line_relax<T, false, true, true> : k_line_relax<T, false, false, true>)
+                              : (zin ? k_line_relax<T, false, true> : k_line_relax<T, false, false>);
+            kern<<<grd, nt, smem, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
             ++h->launches;
         }
         timed_end(h, KIND_LINE, level);
         std::swap(L.p, L.p2);
     }
-    if (walls && nu > 0) side_fill<T>(h, L.g, c, (T*)L.p, (T*)L.p2, nullptr, 0.0, false);
+    if (walls && nu > 0)  // closer to the ghosts' fixed point for the residual that follows
+        for (int r = 0; r < 2; ++r) side_fill<T>(h, L.g, c, (T*)L.p, (T*)L.p2, nullptr, 0.0, false);
 }
 
 template <typename T>
@@ -752,6 +780,8 @@ int validate(const ples_mg_desc* d, ples_mg_handle* h) {
         return fail(h, PLES_MG_BAD_ARG, "ip and kp must be 0 (periodic) or 1 (walls)");
     if ((d->ip || d->kp) && d->solid)
         return fail(h, PLES_MG_BAD_ARG, "an immersed-boundary mask needs periodic x and z (ip = kp = 0)");
+    if ((d->ip || d->kp) && d->smoother == 2)
+        return fail(h, PLES_MG_BAD_ARG, "the TMA-staged smoother needs periodic x and z (ip = kp = 0)");
     if (d->precision != PLES_MG_PREC_FP64 && d->precision != PLES_MG_PREC_MIXED)
         return fail(h, PLES_MG_BAD_ARG, "unknown precision %d", d->precision);
     if (d->coords_layout != PLES_MG_COORDS_NODES && d->coords_layout != PLES_MG_COORDS_GHOSTED8)
@@ -1113,7 +1143,9 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     h->omega = d->omega > 0.0 ? d->omega : (d->smoother != 1 ? 1.3 : 0.8);
     h->nu_pre = d->nu_pre ? d->nu_pre : 2;
     h->nu_post = d->nu_post ? d->nu_post : 2;
-    h->nu_coarse = d->nu_coarse ? d->nu_coarse : 40;
+    // sweeps on a smoothed coarsest level (x / z walls, no dense inverse): 10,
+    // the reference's coarse-level kss; otherwise the coarsest is dense
+    h->nu_coarse = d->nu_coarse ? d->nu_coarse : ((d->ip || d->kp) ? 10 : 40);
     h->inner_cycles = d->inner_cycles ? d->inner_cycles : 5;
     const int jx = d->jx, jy = d->jy, jz = d->jz;
     // nodes (host copy needed for the spacings)

@@ -176,3 +176,29 @@ def test_pressure_step_with_walls_matches_oracle(grid, ip, kp, nproc):
         old[2][:, :, 0], old[2][:, :, jz] = wc[:, :, 0], wc[:, :, jz]
     d0 = np.abs(diver(uc1, vc1, wc1, 1.0)).max()
     assert np.abs(diver(*old, 1.0)).max() <= 1e-8 * d0
+
+
+def test_steep_wall_grid_never_returns_garbage():
+    """x walls on a strongly sheared grid (wall amplitude 0.1, stretching 2.5,
+    the benchmark channel's shape): the wall ghost relation is not
+    contractive there (2(|g12|+|g13|)/(4 g11) > 2 near the bottom wall) and
+    the reference's own solver diverges (the oracle's residual grows by many
+    orders in its first cycles).  The device either reports DIVERGED or
+    returns a field that satisfies the reference's discrete system."""
+    from ples_gb300 import mg
+    x, y, z = S.wavy_channel_grid(32, 16, 32, 0.1, 2.5)
+    rhs = S.divergence_rhs(32, 16, 32, seed=1)
+    orc = Oracle(x, y, z, ip=1, kp=0, islor=1)
+    *_, rr = orc.multi(rhs, eps=1e-13, ficycle=3)
+    assert not (rr < 1.0)
+    with mg.Multigrid(x, y, z, ip=1) as m:
+        try:
+            fi, st = m.solve(rhs, rel_tol=1e-10)
+        except mg.PlesMGError as e:
+            assert e.value.code == mg.DIVERGED
+        else:
+            assert st["status"] == mg.OK
+            r, _ = orc.true_residual(fi, rhs - rhs.mean(), passes=3)
+            assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 1e-8
+        fi, st = m.solve(np.zeros((32, 16, 32), order="F"), rel_tol=1e-10)
+        assert st["status"] == mg.OK
