@@ -79,6 +79,28 @@ module ples_mg_iface
             integer(c_int), value :: code
             type(c_ptr) :: ples_mg_strerror
         end function ples_mg_strerror
+
+        integer(c_int) function ples_mg_step(handle, u, v, w, uc, vc, wc, fi, rel_tol, max_cycles, &
+                                             stats) bind(C, name="ples_mg_step")
+            import :: c_int, c_ptr, c_double, ples_mg_stats
+            type(c_ptr), value :: handle, u, v, w, uc, vc, wc, fi
+            real(c_double), value :: rel_tol
+            integer(c_int), value :: max_cycles
+            type(ples_mg_stats), intent(out) :: stats
+        end function ples_mg_step
+
+        integer(c_int) function ples_mg_potenziale_ibm(handle, fi) bind(C, name="ples_mg_potenziale_ibm")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle, fi
+        end function ples_mg_potenziale_ibm
+
+        integer(c_int) function ples_mg_read_grid(path, lengths, dims, x, y, z) bind(C, name="ples_mg_read_grid")
+            import :: c_int, c_ptr, c_char, c_double
+            character(kind=c_char), dimension(*), intent(in) :: path
+            real(c_double), intent(out) :: lengths(3)
+            integer(c_int), intent(out) :: dims(3)
+            type(c_ptr), value :: x, y, z
+        end function ples_mg_read_grid
     end interface
 
     type(c_ptr), save :: mg_handle = c_null_ptr
@@ -126,5 +148,27 @@ contains
         if (stat /= PLES_MG_OK .and. stat /= PLES_MG_NOT_CONVERGED) error stop 'ples_mg_solve failed'
         ktime = st%outer_iterations
     end subroutine multi_gpu
+
+    !-------------------------------------------------------------------
+    ! the whole pressure step of a time step (contra, diver, multi, gradie,
+    ! vel_up; fsrc/stratiParticle.f03:2845-2937) on the GPU: u, v, w are the
+    ! intermediate Cartesian velocities (0:n1+1,0:n2+1,0:n3+1), uc, vc, wc the
+    ! previous contravariant ones (iniz.f03:103-105 extents on one rank); all
+    ! are updated in place, fi takes the pressure; stop at ||r||/||b|| <= rel_tol
+    subroutine pressure_step_gpu(u, v, w, uc, vc, wc, fi, rel_tol, ficycle, ktime)
+        real(c_double), target, intent(inout) :: u(0:, 0:, 0:), v(0:, 0:, 0:), w(0:, 0:, 0:)
+        real(c_double), target, intent(inout) :: uc(0:, :, :), vc(:, 0:, :), wc(:, :, 0:)
+        real(c_double), target, intent(inout) :: fi(0:, 0:, 0:)
+        real(c_double), intent(in) :: rel_tol
+        integer, intent(in) :: ficycle
+        integer, intent(out) :: ktime
+        type(ples_mg_stats) :: st
+        integer(c_int) :: stat
+
+        stat = ples_mg_step(mg_handle, c_loc(u), c_loc(v), c_loc(w), c_loc(uc), c_loc(vc), c_loc(wc), &
+                            c_loc(fi), rel_tol, int(ficycle, c_int), st)
+        if (stat /= PLES_MG_OK .and. stat /= PLES_MG_NOT_CONVERGED) error stop 'ples_mg_step failed'
+        ktime = st%outer_iterations
+    end subroutine pressure_step_gpu
 
 end module ples_mg_iface
