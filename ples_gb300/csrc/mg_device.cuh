@@ -22,10 +22,12 @@
 // for the reference's full coarsening (sx=sy=sz=2^(n-1)) that is exactly
 // mul_met's t/pot times ppot2.
 //
-// Periodic ghost shell (ip = kp = 0).  Ghost cells with i or k outside the
-// interior hold the periodic image of the interior, for every row j
-// including the two wall ghost rows; every kernel that writes a field keeps
-// the shell consistent, so no separate ghost-copy pass is needed.
+// Ghost shell.  In a periodic direction (ip = 0 / kp = 0, Geom px / pz)
+// ghost cells with i or k outside the interior hold the periodic image of
+// the interior, for every row j including the two wall ghost rows; every
+// kernel that writes a field keeps those images, so no separate copy pass is
+// needed.  In a walled direction the ghosts follow the wall relation and are
+// set by the side fill (outer_device.cuh).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -158,9 +160,9 @@ __device__ __forceinline__ T cell_residual(const Geom& g, const Coef<T>& c, cons
 }
 
 // ---------------------------------------------------------------------------
-// Periodic ghost shell refresh (ip = kp = 0): every ghost cell with i or k
-// outside the interior copies its periodic image, rows j = 0..ny+1.  Used
-// once on fields that arrive from outside (the caller's fi).
+// Periodic ghost shell refresh: every ghost cell with i or k outside the
+// interior in a periodic direction copies its periodic image, rows
+// j = 0..ny+1.  Used once on fields that arrive from outside (the caller's fi).
 template <typename T>
 __device__ __forceinline__ void k_ghost_xz_blk(Geom g, T* __restrict__ p, const Blk& B) {
     const int nxg = g.nx + 2, nyg = g.ny + 2;

@@ -1731,7 +1731,7 @@ int ples_mg_kernel_time(ples_mg_handle* h, double* total_ms, long long* launches
 
 // ---- projection step either side of the solve (the calls around multi at
 // fsrc/stratiParticle.f03:2845-2937: diver, multi, gradie, vel_up), for
-// potenziale = 0, no free surface, periodic x and z, walls in y
+// potenziale = 0, no free surface, walls in y, x and z periodic or walled
 
 }  // extern "C"
 
