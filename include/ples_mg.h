@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define PLES_MG_ABI_VERSION 3
+#define PLES_MG_ABI_VERSION 4
 
 /* status codes */
 enum {
@@ -218,8 +218,9 @@ int ples_mg_read_grid(const char *path, double lengths[3], int dims[3], double *
 /* ---- autotuner ----------------------------------------------------------
  * No counterpart in the reference (its kss, nlevel and omega are fixed
  * inputs).  Times candidate settings on this handle's grid and keeps the
- * fastest: the CTA width of the eta-line smoother per level (128, 256 or 512
- * threads, by kernel time) and then the sweeps per level (nu_pre = nu_post
+ * fastest: the form of the eta-line smoother per level (128, 256 or 512
+ * threads on 32-line tiles, or 1024 for 512 threads on 64-line tiles, by
+ * kernel time) and then the sweeps per level (nu_pre = nu_post
  * in 1..3) and V-cycles per outer iteration (2 to 6), by the time of a
  * whole solve to ||r||/||b|| <= 1e-10 from zero.  rhs (host, (1:jx,1:jy,
  * 1:jz)) or NULL for a pseudo-random compatible one.  Batches created
@@ -227,11 +228,19 @@ int ples_mg_read_grid(const char *path, double lengths[3], int dims[3], double *
 typedef struct {
     int nu;               /* sweeps per level before and after the coarse correction */
     int inner_cycles;     /* V-cycles per FP64 outer iteration */
-    int line_threads[12]; /* smoother CTA width per level (0 past the last level) */
+    int line_threads[12]; /* smoother form per level, as ples_mg_set_line_threads (0 past the last level) */
     double solve_ms;      /* one solve with the chosen setting */
     int candidates;       /* settings timed */
 } ples_mg_tuning;
 int ples_mg_autotune(ples_mg_handle *h, const double *rhs, ples_mg_tuning *out);
+/* Set the form of the eta-line smoother at one level (1-based), as the
+ * autotuner does: 128, 256 or 512 threads per CTA on 32-line tiles, or 1024
+ * for the 64-line-tile form (512 threads; mixed precision, zebra smoother,
+ * x and z periodic, nx of the level even, nz >= 2).  No counterpart in the
+ * reference (its sweeps are scalar loops, multigrid.f03:1939-2290).  BAD_ARG
+ * for another value, a form that does not apply at that level or whose
+ * shared memory does not fit. */
+int ples_mg_set_line_threads(ples_mg_handle *h, int level, int threads);
 
 /* ---- many grids at once ------------------------------------------------
  * No counterpart in the reference, which solves one grid per run.  A batch

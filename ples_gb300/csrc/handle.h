@@ -31,7 +31,11 @@ struct LevelData {
     bool has_cf = false, has_cd = false;
     // TMA-staged zebra smoother (FP32): tensor maps of this level's fields;
     // pA/pB are the buffers behind maps.pA/pB (p and p2 swap every sweep)
-    int line_threads = 256;  // CTA width of the eta-line smoother (128, 256 or 512; autotuned)
+    // CTA width of the eta-line smoother: 128, 256 or 512 threads on 32-line
+    // tiles, or 1024 for the 64-line-tile form (512 threads, k_line_relax_x2);
+    // autotuned
+    int line_threads = 256;
+    bool x2_ok = false;  // the 64-line-tile form applies (FP32, x and z periodic, nx even, nz >= 2)
     bool tma = false;
     void *pA = nullptr, *pB = nullptr;
     ples::LineMaps maps{};

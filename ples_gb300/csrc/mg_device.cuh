@@ -92,6 +92,21 @@ __device__ __forceinline__ T ld(const T* p, long long q) { return __ldg(p + q); 
 template <typename T>
 __device__ __forceinline__ T ld(const T* p, unsigned q) { return __ldg(p + q); }
 
+// 1: the line smoother loads the arrays it reads once per launch with the
+// streaming operator (ld.global.cs: evict-first in L2), so that the rows its
+// odd-i pass reads a second time stay in L2; 0: every load plain
+#ifndef PLES_LINE_L2HINT
+#define PLES_LINE_L2HINT 1
+#endif
+template <typename T>
+__device__ __forceinline__ T ld1(const T* p, unsigned q) {
+#if PLES_LINE_L2HINT
+    return __ldcs(p + q);
+#else
+    return __ldg(p + q);
+#endif
+}
+
 // element offset of (i,j,k) in 32 bits: a box has fewer than 2^31 elements
 // (checked when a handle is created), so kernels that issue many loads per
 // cell form each address with one 32x32->64 multiply-add
@@ -265,16 +280,20 @@ __global__ void k_zero_solid(Geom g, T* __restrict__ p, const uint8_t* __restric
 // drops from 2 nj to about 4 nj / nw + 2 nw dependent steps.  The solution
 // replaces G.  Lanes with mine == false do no arithmetic; every thread must
 // call (the function holds __syncthreads).
-template <typename T>
-__device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int nj, bool mine, T* su, T* sv) {
+// RS: row stride of G / AL / CP (lines per tile); slot: this lane's column
+// in them (the lane itself when negative).
+template <typename T, int RS = 32>
+__device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int nj, bool mine, T* su, T* sv,
+                                           int slot = -1) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int col = slot < 0 ? lane : slot;
     const int len = (nj + nw - 1) / nw;
     const int j0 = min(w * len, nj), j1 = min(j0 + len, nj);
     T u = T(0), v = T(1);
     if (mine)
         for (int j = j0; j < j1; ++j) {
-            const T al = AL[j * 32 + lane];
-            u = G[j * 32 + lane] - al * u;
+            const T al = AL[j * RS + col];
+            u = G[j * RS + col] - al * u;
             v = -al * v;
         }
     su[w * 32 + lane] = u;
@@ -284,16 +303,16 @@ __device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int n
         T d = T(0);
         for (int s = 0; s < w; ++s) d = su[s * 32 + lane] + sv[s * 32 + lane] * d;
         for (int j = j0; j < j1; ++j) {
-            d = G[j * 32 + lane] - AL[j * 32 + lane] * d;
-            G[j * 32 + lane] = d;
+            d = G[j * RS + col] - AL[j * RS + col] * d;
+            G[j * RS + col] = d;
         }
     }
     u = T(0);
     v = T(1);
     if (mine)
         for (int j = j1 - 1; j >= j0; --j) {
-            const T c = CP[j * 32 + lane];
-            u = G[j * 32 + lane] - c * u;
+            const T c = CP[j * RS + col];
+            u = G[j * RS + col] - c * u;
             v = -c * v;
         }
     __syncthreads();  // the forward maps are read by now
@@ -304,8 +323,8 @@ __device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int n
         T x = T(0);
         for (int s = nw - 1; s > w; --s) x = su[s * 32 + lane] + sv[s * 32 + lane] * x;
         for (int j = j1 - 1; j >= j0; --j) {
-            x = G[j * 32 + lane] - CP[j * 32 + lane] * x;
-            G[j * 32 + lane] = x;
+            x = G[j * RS + col] - CP[j * RS + col] * x;
+            G[j * RS + col] = x;
         }
     }
     __syncthreads();
@@ -429,12 +448,16 @@ __device__ __forceinline__ T from_east(T v, T h) {
 // 2160, masks i_dx..i_in of sett.f03) a wall face carries no flux in the
 // relaxed equation (the correction's wall flux is zero), while the ghost
 // cells beyond it still enter the cross terms of the other faces.
-template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false>
+// RS, slot: as in seg_thomas; ws / nws: the row segment this warp builds and
+// the number of segments (by default the warp's index among the CTA's warps).
+template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false, int RS = 32>
 __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, const T* __restrict__ cpa,
                                            const T* __restrict__ pin, const T* __restrict__ pk,
                                            const T* __restrict__ rh, T omega, int zk, int i, int k, bool odd, T* G,
-                                           T* AL, T* CP) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+                                           T* AL, T* CP, int ws = -1, int nws = 0, int slot = -1) {
+    const int lane = threadIdx.x & 31;
+    const int w = ws < 0 ? (int)(threadIdx.x >> 5) : ws, nw = ws < 0 ? (int)(blockDim.x >> 5) : nws;
+    const int sc = slot < 0 ? lane : slot;
     const int nj = g.ny + 2, ny = g.ny;
     const int len = (nj + nw - 1) / nw;
     const int j0 = min(w * len, nj), j1 = min(j0 + len, nj);
@@ -493,17 +516,19 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
         T a2v = T(0), b21v = T(0), b23v = T(0), cpv = T(0);
         T a1e = T(0), b12v = T(0), b13v = T(0), a1h = T(0), b12h = T(0), b13h = T(0);
         T a3f = T(0), a3b = T(0), b31v = T(0), b31b = T(0), b32v = T(0), b32b = T(0), rhv = T(0);
+        // (ld1: arrays this launch reads once; a1, b12, b21, b31 and c' are
+        // read again by the odd-i pass and stay plain)
         if (act && j <= ny) {
-            a2v = ld(c.a2, q);
+            a2v = ld1(c.a2, q);
             b21v = ld(c.b21, q);
-            b23v = ld(c.b23, q);
+            b23v = ld1(c.b23, q);
             cpv = ld(cpa, q);
         }
         if (act && j >= 1 && j <= ny) {
-            a1e = ld(c.a1, q); b12v = ld(c.b12, q); b13v = ld(c.b13, q);
-            a3f = ld(c.a3, q); b31v = ld(c.b31, q); b32v = ld(c.b32, q);
-            a3b = ld(c.a3, q - sk); b31b = ld(c.b31, q - sk); b32b = ld(c.b32, q - sk);
-            rhv = ld(rh, q);
+            a1e = ld(c.a1, q); b12v = ld(c.b12, q); b13v = ld1(c.b13, q);
+            a3f = ld1(c.a3, q); b31v = ld(c.b31, q); b32v = ld1(c.b32, q);
+            a3b = ld1(c.a3, q - sk); b31b = ld(c.b31, q - sk); b32b = ld1(c.b32, q - sk);
+            rhv = ld1(rh, q);
             if (lane == 0) { a1h = ld(c.a1, q - 1); b12h = ld(c.b12, q - 1); b13h = ld(c.b13, q - 1); }
         }
         // ... then the pressure rows j+1 of the three planes
@@ -600,10 +625,10 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
             // line operator of row j, T x = omega f + (1 - omega) T p_old
             // gives x = p_old + omega (T^-1 f - p_old) (identity rows keep
             // T p_old = p_old)
-            G[j * 32 + lane] = (ZIN ? omega * f : omega * f + (T(1) - omega) * tp) * im;
-            AL[j * 32 + lane] = a * im;
+            G[j * RS + sc] = (ZIN ? omega * f : omega * f + (T(1) - omega) * tp) * im;
+            AL[j * RS + sc] = a * im;
             // odd lanes keep 1/m here until their x-neighbour terms are added
-            CP[j * 32 + lane] = odd ? im : (j == ny + 1 ? T(0) : cpv);
+            CP[j * RS + sc] = odd ? im : (j == ny + 1 ? T(0) : cpv);
         }
         a2s = a2v; b21s = b21v; b23s = b23v; cps = cpv;
     }
@@ -640,14 +665,14 @@ __device__ __forceinline__ void odd_x_rows(const Geom& g, const Coef<T>& c, cons
         for (int u = 0; u < kXR; ++u) {
             const int j = min(jb + u, j1 - 1);
             const unsigned q = q0 + (unsigned)j * sj;
-            a1[u] = act ? ld(c.a1, q) : T(0);
-            b12[u] = act ? ld(c.b12, q) : T(0);
+            a1[u] = act ? ld1(c.a1, q) : T(0);  // their last read in this launch
+            b12[u] = act ? ld1(c.b12, q) : T(0);
             a1h[u] = act && lane == 0 ? ld(c.a1, q - 1) : T(0);
             b12h[u] = act && lane == 0 ? ld(c.b12, q - 1) : T(0);
-            b21[u] = mine ? ld(c.b21, q) : T(0);
-            b31[u] = mine ? ld(c.b31, q) : T(0);
-            b31b[u] = mine ? ld(c.b31, q - sk) : T(0);
-            cpv[u] = mine ? ld(cpa, q) : T(0);
+            b21[u] = mine ? ld1(c.b21, q) : T(0);
+            b31[u] = mine ? ld1(c.b31, q) : T(0);
+            b31b[u] = mine ? ld1(c.b31, q - sk) : T(0);
+            cpv[u] = mine ? ld1(cpa, q) : T(0);
         }
 #pragma unroll
         for (int v = 0; v < kXR + 2; ++v) {  // old west column, rows jb-1 .. jb+kXR
@@ -803,6 +828,121 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? PLES_LINE_MIN_BLOCKS : 2
                                                     T* __restrict__ pout, const T* __restrict__ rh, T omega,
                                                     int kpar, int zk) {
     k_line_relax_blk<T, ZEBRA, ZIN, WALLS>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
+}
+
+// ---------------------------------------------------------------------------
+// The zebra smoother on 64-line tiles (FP32, x and z periodic, nx even): the
+// same sweep as k_line_relax<float, zebra> with the tile edges, where the x
+// coupling is Jacobi, every 64 lines instead of 32.  A CTA of 16 warps owns
+// the lines i0..i0+63 of one plane, i0 = 64 b + 1 (odd).  Warps 0-7 build
+// the rows of lines i0..i0+31 and warps 8-15 those of i0+32..i0+63 (one
+// line per lane, build_rows unchanged).  G / AL / CP hold 64 columns per row:
+// the odd-i line i0+2l in column l, the even-i line i0+2l+1 in column 32+l.
+// So each half of the zebra has one line per lane of every warp, and all 16
+// warps solve it (seg_thomas over 16 row segments) with every lane busy;
+// the odd-i lines' x-terms (odd_x_pairs) and the store (one pair per lane,
+// 8-byte stores) likewise.
+
+// Second half: lane l adds to line i = i0+2l (column l) its x-neighbour
+// terms with the new even-i values beside it, i-1 in column 32+l-1 (lane 0:
+// outside the tile, old field) and i+1 in column 32+l (new while i+1 <= nx);
+// rows of this warp's segment in order with a sliding window of the
+// neighbours' rows j-1, j, j+1.  Then CP(j) changes from 1/m(j) to c'(j).
+// Same terms and order as odd_x_rows.
+template <bool ZIN>
+__device__ __forceinline__ void odd_x_pairs(const Geom& g, const Coef<float>& c, const float* __restrict__ cpa,
+                                            const float* __restrict__ pin, float omega, float* G, float* CP,
+                                            int i, int k) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nj = g.ny + 2, ny = g.ny;
+    const int len = (nj + nw - 1) / nw;
+    const int j0 = min(w * len, nj), j1 = min(j0 + len, nj);
+    if (i > g.nx || j0 >= j1) return;
+    const unsigned sj = (unsigned)g.sj, sk = (unsigned)g.sk, q0 = at32(g, i, 0, k);
+    const bool west_in = lane > 0, east_in = i + 1 <= g.nx;
+    const int cw = 32 + lane - 1, ce = 32 + lane;
+    auto WV = [&](int jj) -> float {
+        if (west_in) return G[jj * 64 + cw];
+        return ZIN ? 0.f : ld(pin, q0 + (unsigned)jj * sj - 1u);
+    };
+    auto EV = [&](int jj) -> float {
+        if (east_in) return G[jj * 64 + ce];
+        return ZIN ? 0.f : ld(pin, q0 + (unsigned)jj * sj + 1u);
+    };
+    float wm = j0 > 0 ? WV(j0 - 1) : 0.f, w0 = WV(j0), em = j0 > 0 ? EV(j0 - 1) : 0.f, e0 = EV(j0);
+    float b21s = j0 >= 1 ? ld(c.b21, q0 + (unsigned)(j0 - 1) * sj) : 0.f;
+    for (int j = j0; j < j1; ++j) {
+        const unsigned q = q0 + (unsigned)j * sj;
+        const float a1e = ld1(c.a1, q), b12e = ld1(c.b12, q), a1w = ld(c.a1, q - 1u), b12w = ld(c.b12, q - 1u);
+        const float b21 = ld1(c.b21, q), b31f = ld1(c.b31, q), b31k = ld1(c.b31, q - sk), cpv = ld1(cpa, q);
+        const float wp = j < nj - 1 ? WV(j + 1) : 0.f, ep = j < nj - 1 ? EV(j + 1) : 0.f;
+        float tx;
+        if (j == 0) {
+            tx = -b21 * (ep + e0 - wp - w0);
+        } else if (j == ny + 1) {
+            tx = b21s * (e0 + em - w0 - wm);
+        } else {
+            tx = a1e * e0 + a1w * w0 + b12e * (ep - em) - b12w * (wp - wm) + b21 * (ep + e0 - wp - w0) -
+                 b21s * (e0 + em - w0 - wm) + (b31f - b31k) * (e0 - w0);
+        }
+        const float im = CP[j * 64 + lane];
+        G[j * 64 + lane] -= omega * tx * im;
+        CP[j * 64 + lane] = j == ny + 1 ? 0.f : cpv;
+        wm = w0; w0 = wp; em = e0; e0 = ep;
+        b21s = b21;
+    }
+}
+
+// the pair (i, i+1) of row j, plane k (i odd, i+1 <= nx) with its periodic
+// images (store_periodic for two cells; nx even, nz >= 2)
+__device__ __forceinline__ void store_pair(const Geom& g, float* p, int i, int j, int k, float vo, float ve) {
+    const long long q = g.at(i, j, k);
+    *reinterpret_cast<float2*>(p + q) = make_float2(vo, ve);
+    const int gk = !g.pz ? -1 : (k == g.nz ? 0 : (k == 1 ? g.nz + 1 : -1));
+    if (gk >= 0) *reinterpret_cast<float2*>(p + g.at(i, j, gk)) = make_float2(vo, ve);
+    if (g.px && i == 1) {
+        p[g.at(g.nx + 1, j, k)] = vo;
+        if (gk >= 0) p[g.at(g.nx + 1, j, gk)] = vo;
+    }
+    if (g.px && i + 1 == g.nx) {
+        p[g.at(0, j, k)] = ve;
+        if (gk >= 0) p[g.at(0, j, gk)] = ve;
+    }
+}
+
+// Shared memory: 3 arrays [ny+2][64] and the segment maps [2][16][32].
+template <bool ZIN>
+__global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c, const float* __restrict__ cpa,
+                                                          const float* __restrict__ pin, const float* __restrict__ pk,
+                                                          float* __restrict__ pout, const float* __restrict__ rh,
+                                                          float omega, int kpar, int zk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nj = g.ny + 2;
+    float* G = reinterpret_cast<float*>(smem_raw);
+    float* AL = G + nj * 64;
+    float* CP = AL + nj * 64;
+    float* SU = CP + nj * 64;
+    float* SV = SU + 16 * 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int k = 2 * blockIdx.y + 1 + kpar;
+    if (k > g.nz) return;
+    const int i0 = blockIdx.x * 64 + 1;
+    // phase 1: line L = 32 (w / 8) + lane of the tile, row segment w % 8 of 8
+    const int L = 32 * (w >> 3) + lane;
+    const int ib = i0 + L;
+    const int colb = (L & 1) ? 32 + (L >> 1) : (L >> 1);
+    build_rows<float, true, ZIN, false, 64>(g, c, cpa, pin, pk, rh, omega, zk, ib, k, (ib & 1) != 0, G, AL, CP,
+                                             w & 7, 8, colb);
+    // the lane's two lines in the solve phases: io = i0 + 2 lane (odd i,
+    // column lane) and io + 1 (even i, column 32 + lane)
+    const int io = i0 + 2 * lane;
+    __syncthreads();
+    seg_thomas<float, 64>(G, AL, CP, nj, io + 1 <= g.nx, SU, SV, 32 + lane);  // the even-i lines first
+    odd_x_pairs<ZIN>(g, c, cpa, pin, omega, G, CP, io, k);
+    __syncthreads();
+    seg_thomas<float, 64>(G, AL, CP, nj, io <= g.nx, SU, SV, lane);
+    if (io <= g.nx)
+        for (int j = w; j < nj; j += 16) store_pair(g, pout, io, j, k, G[j * 64 + lane], G[j * 64 + 32 + lane]);
 }
 
 // ---------------------------------------------------------------------------

@@ -317,6 +317,18 @@ size_t line_smem(const Geom& g, int threads = 256) {
     return (3 * (size_t)(g.ny + 2) + 2 * (size_t)(threads / 32)) * 32 * sizeof(T);
 }
 
+// the same for the 64-line-tile form (three [ny+2][64] arrays, 16 warps' maps)
+inline size_t line_smem_x2(const Geom& g) { return (3 * (size_t)(g.ny + 2) * 64 + 2 * 16 * 32) * sizeof(float); }
+
+int set_x2_smem_attr(ples_mg_handle* h, size_t smem) {
+    static size_t current = 0;
+    if (smem <= current) return 0;
+    current = smem;
+    CK(cudaFuncSetAttribute(k_line_relax_x2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_x2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return 0;
+}
+
 // the dynamic shared-memory limit is a per-function attribute shared by all
 // handles of the process: only ever raise it
 template <typename T>
@@ -436,7 +448,8 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
     if (zero && nu == 0) cudaMemsetAsync(L.p, 0, sizeof(T) * (size_t)L.g.n, h->st);
     const Coef<T> c = coef_of<T>(L);
     const T om = T(h->omega);
-    const int nt = h->smoother == 1 ? std::min(L.line_threads, 256) : L.line_threads;
+    const bool x2 = std::is_same<T, float>::value && h->smoother == 0 && L.line_threads == 1024 && L.x2_ok;
+    const int nt = h->smoother == 1 ? std::min(L.line_threads, 256) : std::min(L.line_threads, 512);
     const size_t smem = line_smem<T>(L.g, nt);
     const T* cp = (const T*)L.cp;
     const bool walls = !L.g.px || !L.g.pz;
@@ -465,6 +478,17 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
                     k_line_relax_tma<false><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 1, 0, a_in,
                                                                       a_out, h->dflag);
                 }
+                h->launches += 2;
+                staged = true;
+            }
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            if (x2) {  // zebra on 64-line tiles
+                dim3 grd((L.g.nx + 63) / 64, (L.g.nz + 1) / 2);
+                const size_t sm = line_smem_x2(L.g);
+                auto kern = zin ? k_line_relax_x2<true> : k_line_relax_x2<false>;
+                kern<<<grd, 512, sm, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
+                kern<<<grd, 512, sm, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
                 h->launches += 2;
                 staged = true;
             }
@@ -1272,6 +1296,17 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
             const size_t sw = mixed ? line_smem<float>(L.g, 512) : line_smem<double>(L.g, 512);
             L.line_threads = ctas < 2 * 152 && sw <= 227 * 1024 ? 512 : 256;
         }
+        // the 64-line-tile form: FP32 zebra with periodic x and z, nx even
+        L.x2_ok = mixed && h->smoother == 0 && L.g.px && L.g.pz && L.g.nx % 2 == 0 && L.g.nz >= 2 &&
+                  line_smem_x2(L.g) <= 227 * 1024;
+        if (L.x2_ok) {
+            if ((rc = set_x2_smem_attr(h, line_smem_x2(L.g)))) return rc;
+            // by default where its launch has at least 96 CTAs: measured
+            // faster on GB300 at 256x128x256 (238 -> 213 us per sweep) and
+            // 128x64x128, slower at 64x32x64 (32 CTAs)
+            const long long c2 = (long long)((L.g.nx + 63) / 64) * ((L.g.nz + 1) / 2);
+            if (c2 >= 96) L.line_threads = 1024;
+        }
         // room for the 16-warp form where it fits
         sm = std::max(sm, mixed ? line_smem<float>(L.g, 512) : line_smem<double>(L.g, 512));
         smem_max = std::max(smem_max, std::min(sm, (size_t)227 * 1024));
@@ -2011,8 +2046,28 @@ int ples_mg_step(ples_mg_handle* h, double* u, double* v, double* w, double* uc,
     });
 }
 
-// Autotuner: first the CTA width of the eta-line smoother per level (128 or
-// 256 threads; the kernel's own time, CUDA events), then the sweep count per
+int ples_mg_set_line_threads(ples_mg_handle* h, int level, int threads) {
+    if (!h) return PLES_MG_BAD_ARG;
+    if (level < 1 || level > h->nlev) return fail(h, PLES_MG_BAD_ARG, "level %d outside 1..%d", level, h->nlev);
+    LevelData& L = h->L[level - 1];
+    const bool mixed = h->d.precision == PLES_MG_PREC_MIXED;
+    size_t need = 0;
+    if (threads == 1024) {
+        if (!L.x2_ok) return fail(h, PLES_MG_BAD_ARG, "the 64-line-tile smoother does not apply at level %d", level);
+        need = line_smem_x2(L.g);
+    } else if (threads == 128 || threads == 256 || threads == 512) {
+        need = mixed ? line_smem<float>(L.g, threads) : line_smem<double>(L.g, threads);
+    } else {
+        return fail(h, PLES_MG_BAD_ARG, "smoother form %d is not 128, 256, 512 or 1024", threads);
+    }
+    if (need > 227 * 1024) return fail(h, PLES_MG_BAD_ARG, "smoother form %d needs %zu B of shared memory", threads, need);
+    L.line_threads = threads;
+    return PLES_MG_OK;
+}
+
+// Autotuner: first the form of the eta-line smoother per level (128, 256 or
+// 512 threads on 32-line tiles, 1024 for the 64-line tiles; the kernel's own
+// time, CUDA events), then the sweep count per
 // level and the V-cycles per outer iteration (time of whole solves to
 // ||r||/||b|| <= 1e-10 from zero).  The fastest setting is kept in the handle.
 int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) {
@@ -2073,9 +2128,11 @@ int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) 
         for (int n = 0; n < nsmooth; ++n) {
             double best = 1e300;
             int bt = h->L[n].line_threads;
-            for (int t : {128, 256, 512}) {
+            for (int t : {128, 256, 512, 1024}) {
                 const LevelData& Ln = h->L[n];
-                const size_t need = h->d.precision == PLES_MG_PREC_MIXED ? line_smem<float>(Ln.g, t)
+                if (t == 1024 && !Ln.x2_ok) continue;
+                const size_t need = t == 1024 ? line_smem_x2(Ln.g)
+                                    : h->d.precision == PLES_MG_PREC_MIXED ? line_smem<float>(Ln.g, t)
                                                                           : line_smem<double>(Ln.g, t);
                 if (need > 227 * 1024) continue;
                 h->L[n].line_threads = t;

@@ -72,6 +72,7 @@ def test_null_arguments():
     h = C.c_void_p()
     assert lib.ples_mg_create(None, C.byref(h)) == mg.BAD_ARG
     lib.ples_mg_destroy(None)
+    assert lib.ples_mg_set_line_threads(None, 1, 256) == mg.BAD_ARG
 
 
 def test_no_device_reported_on_cpu_host():

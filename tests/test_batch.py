@@ -143,7 +143,7 @@ def test_autotune_then_batch(cases):
     tuned = [m.autotune(c[3]) for m, c in zip(members, sub)]
     for t in tuned:
         assert t["nu"] in (1, 2, 3) and t["inner_cycles"] in (2, 3, 4, 5, 6)
-        assert set(t["line_threads"]) <= {128, 256, 512} and t["candidates"] >= 13
+        assert set(t["line_threads"]) <= {128, 256, 512, 1024} and t["candidates"] >= 13
     with mg.Batch(members) as b:
         fis, sts = b.solve([c[3] for c in sub], rel_tol=REL_TOL)
     for m, c, fi, st in zip(members, sub, fis, sts):

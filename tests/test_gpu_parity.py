@@ -233,6 +233,41 @@ def test_staged_and_plain_zebra_agree(case0):
     assert l2 <= SOL_TOL and mx <= SOL_TOL
 
 
+def test_64_line_tiles_match_oracle_and_32_line_tiles():
+    """The zebra smoother on 64-line tiles (k_line_relax_x2), set at every
+    level where it applies, converges to the oracle's solution: one full
+    tile (64), a full and a part tile (96), one part tile (40).  Levels with
+    an odd nx reject it.  The 32-line form on the same handle gives the
+    same solution within 1e-9."""
+    for dims in ((64, 32, 64), (96, 16, 48), (40, 12, 20)):
+        x, y, z = S.wavy_channel_grid(*dims, 0.05, 1.5)
+        rhs = S.divergence_rhs(*dims, seed=4)
+        orc = Oracle(x, y, z, islor=1)
+        fo, *_ = orc.multi(rhs, eps=1e-13, ficycle=400)
+        with mg.Multigrid(x, y, z) as m:
+            set_at = []
+            for lev in range(1, m.nlevel + 1):
+                nx, _, nz = m.dims(lev)
+                if nx % 2 or nz < 2:
+                    with pytest.raises(mg.PlesMGError):
+                        m.set_line_threads(lev, 1024)
+                    continue
+                m.set_line_threads(lev, 1024)
+                set_at.append(lev)
+            assert 1 in set_at
+            fi, st = m.solve(rhs, rel_tol=REL_TOL)
+            for lev in set_at:
+                m.set_line_threads(lev, 256)
+            fi32, st32 = m.solve(rhs, rel_tol=REL_TOL)
+        assert st["status"] == mg.OK and st32["status"] == mg.OK, (dims, st, st32)
+        l2, mx = _rel(_zm(fi), _zm(fo))
+        assert l2 <= SOL_TOL and mx <= SOL_TOL, (dims, l2, mx)
+        r, _ = orc.true_residual(fi, rhs)
+        assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 2e-10
+        l2, mx = _rel(_zm(fi), _zm(fi32))
+        assert l2 <= 1e-9 and mx <= 1e-9, (dims, l2, mx)
+
+
 def test_odd_level_counts_and_small_grids():
     # (40, 12, 20): partial 32-lane tiles, rows not a multiple of the 8-row
     # blocks and planes not a multiple of the 8-plane walks of the kernels

@@ -50,12 +50,18 @@ def test_empty_mask_assembly_matches_reference_solver(case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64", "mixed-64-line-tiles"])
 def test_device_masked_solve_matches_oracle(case, precision):
     from ples_gb300 import mg
     ref = masked_solve(case["orc"], case["rhs"], case["solid"])
     fluid = ~case["solid"]
-    with mg.Multigrid(case["x"], case["y"], case["z"], precision=precision, solid=case["solid"]) as m:
+    prec = precision.split("-")[0]
+    with mg.Multigrid(case["x"], case["y"], case["z"], precision=prec, solid=case["solid"]) as m:
+        if precision.endswith("tiles"):  # the 64-line-tile smoother at every level with nx even
+            for lev in range(1, m.nlevel + 1):
+                nx, _, nz = m.dims(lev)
+                if nx % 2 == 0 and nz >= 2:
+                    m.set_line_threads(lev, 1024)
         fi, st = m.solve(case["rhs"], rel_tol=1e-10, max_cycles=300)
     assert st["status"] == mg.OK and st["rel_residual"] <= 1e-10, st
     p = fi[1:-1, 1:-1, 1:-1]
