@@ -584,11 +584,14 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
     avg_launch_s = kms / 1e3 / kn if kn else None
     achieved = LINE_BYTES_PER_CELL * cells / avg_launch_s / 1e9 if avg_launch_s else None
     traffic = None
+    kernel = "eta-line smoother level 1, one sweep = 2 launches (k parities)"
     prof = os.path.join(ROOT, "profiles", f"line_relax_{args.workload}.json")
     if os.path.exists(prof):
         try:
             # per timed unit: one sweep = both k-parity launches
-            traffic = json.load(open(prof)).get("dram_bytes_per_sweep")
+            pj = json.load(open(prof))
+            traffic = pj.get("dram_bytes_per_sweep")
+            kernel = pj.get("kernel", kernel)
         except Exception:
             traffic = None
     cpu = None
@@ -614,7 +617,7 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic,
-                     "kernel": "k_line_relax<float,zebra> level 1, one sweep = 2 launches (k parities)",
+                     "kernel": kernel,
                      "launches_timed": kn, "avg_launch_ms": avg_launch_s * 1e3 if avg_launch_s else None,
                      "peak_source": peak_kind,
                      "bytes_per_launch": LINE_BYTES_PER_CELL * cells},
