@@ -580,7 +580,7 @@ int build_steps(ples_mg_batch* b) {
     for (int i = 0; i < nm; ++i) {
         ples_mg_handle* h = b->mem[i];
         for (int n = 0; n < h->nlev; ++n)
-            b->smem_line = std::max(b->smem_line, (3 * (size_t)(h->L[n].g.ny + 2) + 2 * 8) * 32 * sizeof(float));
+            b->smem_line = std::max(b->smem_line, (3 * (size_t)(h->L[n].g.ny + 2) + 4 * 8) * 32 * sizeof(float));
         b->smem_dense = std::max(b->smem_dense, (size_t)h->coarse_n * sizeof(float));
     }
     return PLES_MG_OK;

@@ -281,10 +281,14 @@ __global__ void k_zero_solid(Geom g, T* __restrict__ p, const uint8_t* __restric
 // replaces G.  Lanes with mine == false do no arithmetic; every thread must
 // call (the function holds __syncthreads).
 // RS: row stride of G / AL / CP (lines per tile); slot: this lane's column
-// in them (the lane itself when negative).
-template <typename T, int RS = 32>
+// in them (the lane itself when negative).  The folds over the maps of the
+// segments before / after a warp's own are unrolled to NWMAX (the most warps
+// a CTA has), so their shared-memory loads issue ahead of the FMA chain.
+// su2 / sv2: a second map buffer for the backward maps, which saves the
+// barrier that otherwise protects the forward maps (null: one buffer).
+template <typename T, int RS = 32, int NWMAX = 16>
 __device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int nj, bool mine, T* su, T* sv,
-                                           int slot = -1) {
+                                           int slot = -1, T* su2 = nullptr, T* sv2 = nullptr) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int col = slot < 0 ? lane : slot;
     const int len = (nj + nw - 1) / nw;
@@ -301,7 +305,9 @@ __device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int n
     __syncthreads();
     if (mine) {
         T d = T(0);
-        for (int s = 0; s < w; ++s) d = su[s * 32 + lane] + sv[s * 32 + lane] * d;
+#pragma unroll
+        for (int s = 0; s < NWMAX; ++s)
+            if (s < w) d = su[s * 32 + lane] + sv[s * 32 + lane] * d;
         for (int j = j0; j < j1; ++j) {
             d = G[j * RS + col] - AL[j * RS + col] * d;
             G[j * RS + col] = d;
@@ -315,13 +321,17 @@ __device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int n
             u = G[j * RS + col] - c * u;
             v = -c * v;
         }
-    __syncthreads();  // the forward maps are read by now
-    su[w * 32 + lane] = u;
-    sv[w * 32 + lane] = v;
+    T* bu = su2 ? su2 : su;
+    T* bv = su2 ? sv2 : sv;
+    if (!su2) __syncthreads();  // the forward maps are read by now
+    bu[w * 32 + lane] = u;
+    bv[w * 32 + lane] = v;
     __syncthreads();
     if (mine) {
         T x = T(0);
-        for (int s = nw - 1; s > w; --s) x = su[s * 32 + lane] + sv[s * 32 + lane] * x;
+#pragma unroll
+        for (int s = NWMAX - 1; s >= 0; --s)
+            if (s < nw && s > w) x = bu[s * 32 + lane] + bv[s * 32 + lane] * x;
         for (int j = j1 - 1; j >= j0; --j) {
             x = G[j * RS + col] - CP[j * RS + col] * x;
             G[j * RS + col] = x;
@@ -550,8 +560,10 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
             pf_l2(c.a3, qn); pf_l2(c.b31, qn); pf_l2(c.b32, qn);
             pf_l2(c.a3, qn - sk); pf_l2(c.b31, qn - sk); pf_l2(c.b32, qn - sk);
             pf_l2(rh, qn); pf_l2(cpa, qn);
-            if (!ZIN) pf_l2(pin, qn + sj);
-            if (!kz) { pf_l2(pk, qn + sj + sk); pf_l2(pk, qn + sj - sk); }
+            if (j + PLES_LINE_PF_ROWS + 1 < nj) {  // the row after stays inside the plane
+                if (!ZIN) pf_l2(pin, qn + sj);
+                if (!kz) { pf_l2(pk, qn + sj + sk); pf_l2(pk, qn + sj - sk); }
+            }
         }
 #endif
         if (!ZIN) {
@@ -781,7 +793,7 @@ __device__ __forceinline__ void relax_store(const Geom& g, const T* __restrict__
 //         Own-plane old values come from pin, k+-1 planes from pk (= pin for
 //         the first parity, = pout for the second); output to pout.
 // ZIN: pin is identically zero (first sweep of a correction); zk: pk is too.
-// Shared memory: 3 arrays [ny+2][32] and the segment maps [2][warps][32].
+// Shared memory: 3 arrays [ny+2][32] and the segment maps [4][warps][32].
 template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false>
 __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __restrict__ cpa,
                                                     const T* __restrict__ pin, const T* __restrict__ pk,
@@ -801,14 +813,16 @@ __device__ __forceinline__ void k_line_relax_blk(Geom g, Coef<T> c, const T* __r
     const bool act = i <= g.nx;
     const bool odd = ZEBRA && (i & 1);  // updated in the second half
     build_rows<T, ZEBRA, ZIN, WALLS>(g, c, cpa, pin, pk, rh, omega, zk, i, k, odd, G, AL, CP);
-    T* SU = CP + nj * 32;  // segment maps of the parallel Thomas solve
+    T* SU = CP + nj * 32;  // segment maps of the parallel Thomas solve (forward, backward)
     T* SV = SU + nw * 32;
+    T* SU2 = SV + nw * 32;
+    T* SV2 = SU2 + nw * 32;
     const int nhalf = ZEBRA ? 2 : 1;
     for (int half = 0; half < nhalf; ++half) {
         const bool mine = act && (!ZEBRA || ((i & 1) == half));
         if (ZEBRA && half == 1) odd_x_rows<T, ZIN, WALLS>(g, c, cpa, pin, omega, G, CP, i, k);
         __syncthreads();
-        seg_thomas(G, AL, CP, nj, mine, SU, SV);
+        seg_thomas(G, AL, CP, nj, mine, SU, SV, -1, SU2, SV2);
         if (mine) store_rows(g, pout, G, i, k);
         if (ZEBRA) __syncthreads();
     }
@@ -910,7 +924,7 @@ __device__ __forceinline__ void store_pair(const Geom& g, float* p, int i, int j
     }
 }
 
-// Shared memory: 3 arrays [ny+2][64] and the segment maps [2][16][32].
+// Shared memory: 3 arrays [ny+2][64] and the segment maps [4][16][32].
 template <bool ZIN>
 __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c, const float* __restrict__ cpa,
                                                           const float* __restrict__ pin, const float* __restrict__ pk,
@@ -923,6 +937,8 @@ __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c,
     float* CP = AL + nj * 64;
     float* SU = CP + nj * 64;
     float* SV = SU + 16 * 32;
+    float* SU2 = SV + 16 * 32;
+    float* SV2 = SU2 + 16 * 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int k = 2 * blockIdx.y + 1 + kpar;
     if (k > g.nz) return;
@@ -937,10 +953,10 @@ __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c,
     // column lane) and io + 1 (even i, column 32 + lane)
     const int io = i0 + 2 * lane;
     __syncthreads();
-    seg_thomas<float, 64>(G, AL, CP, nj, io + 1 <= g.nx, SU, SV, 32 + lane);  // the even-i lines first
+    seg_thomas<float, 64>(G, AL, CP, nj, io + 1 <= g.nx, SU, SV, 32 + lane, SU2, SV2);  // the even-i lines first
     odd_x_pairs<ZIN>(g, c, cpa, pin, omega, G, CP, io, k);
     __syncthreads();
-    seg_thomas<float, 64>(G, AL, CP, nj, io <= g.nx, SU, SV, lane);
+    seg_thomas<float, 64>(G, AL, CP, nj, io <= g.nx, SU, SV, lane, SU2, SV2);
     if (io <= g.nx)
         for (int j = w; j < nj; j += 16) store_pair(g, pout, io, j, k, G[j * 64 + lane], G[j * 64 + 32 + lane]);
 }

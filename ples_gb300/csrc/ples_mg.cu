@@ -314,11 +314,11 @@ void ghost_xz(ples_mg_handle* h, const Geom& g, T* p) {
 // G, alpha, c' rows and the segment maps of one CTA of the line smoother
 template <typename T>
 size_t line_smem(const Geom& g, int threads = 256) {
-    return (3 * (size_t)(g.ny + 2) + 2 * (size_t)(threads / 32)) * 32 * sizeof(T);
+    return (3 * (size_t)(g.ny + 2) + 4 * (size_t)(threads / 32)) * 32 * sizeof(T);
 }
 
 // the same for the 64-line-tile form (three [ny+2][64] arrays, 16 warps' maps)
-inline size_t line_smem_x2(const Geom& g) { return (3 * (size_t)(g.ny + 2) * 64 + 2 * 16 * 32) * sizeof(float); }
+inline size_t line_smem_x2(const Geom& g) { return (3 * (size_t)(g.ny + 2) * 64 + 4 * 16 * 32) * sizeof(float); }
 
 int set_x2_smem_attr(ples_mg_handle* h, size_t smem) {
     static size_t current = 0;
