@@ -80,8 +80,24 @@ __global__ void k_box_nonzero(long long n, const double* __restrict__ x, int* __
     k_box_nonzero_blk(n, x, flag, hw_blk());
 }
 
-__global__ void k_sum_interior(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum) {
-    k_sum_interior_blk(g, a, squares, psum, hw_blk());
+// partial sums (or sums of squares) of the interior cells, one per block;
+// each thread walks kSumPlanes planes of its (i, j) column
+constexpr int kSumPlanes = 8;
+__global__ void k_sum_interior_z(Geom g, const double* __restrict__ a, int squares, double* __restrict__ psum) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + tx + 1;
+    const int j = blockIdx.y * (kRedThreads / 32) + ty + 1;
+    const int k0 = blockIdx.z * kSumPlanes + 1;
+    double s = 0.0, m = 0.0;
+    if (i <= g.nx && j <= g.ny) {
+        double v[kSumPlanes];
+#pragma unroll
+        for (int u = 0; u < kSumPlanes; ++u) v[u] = k0 + u <= g.nz ? a[g.at(i, j, k0 + u)] : 0.0;
+#pragma unroll
+        for (int u = 0; u < kSumPlanes; ++u) s += squares ? v[u] * v[u] : v[u];
+    }
+    block_reduce_sum_max(s, m);
+    if (threadIdx.x == 0) psum[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s;
 }
 
 // deterministic final reduction of n partials (sum of a, max of bmax)
@@ -588,7 +604,8 @@ dim3 red_grid(const Geom& g) { return dim3((g.nx + 31) / 32, (g.ny + kRedThreads
 int sum_interior(ples_mg_handle* h, const double* a, int squares, double* out) {
     const Geom& g = h->L[0].g;
     dim3 grd = red_grid(g);
-    k_sum_interior<<<grd, kRedThreads, 0, h->st>>>(g, a, squares, h->part_a);
+    grd.z = (g.nz + kSumPlanes - 1) / kSumPlanes;  // fewer partials than red_grid's, same buffer
+    k_sum_interior_z<<<grd, kRedThreads, 0, h->st>>>(g, a, squares, h->part_a);
     ++h->launches;
     CK(cudaGetLastError());
     double r[2];
