@@ -7,8 +7,9 @@ shared object under ples_gb300/_build/:
   csrc/ples_mg.cu  -- stencil kernels, V-cycle driver and the C ABI
   csrc/batch.cu    -- batched solves of many grids and the request server
   csrc/grid_io.cpp -- reader of PLES's grid file (host code)
-The library depends on the CUDA runtime only (statically linked); PyTorch is
-not needed to build or load it.
+The library depends on the CUDA runtime only (statically linked; NVTX ranges
+come from the toolkit's header-only NVTX v3); PyTorch is not needed to build
+or load it.
 """
 
 from __future__ import annotations
@@ -70,7 +71,7 @@ def build(force=False, verbose=False, extra=()):
             print(out.decode(errors="replace"), file=sys.stderr)
         objs.append(obj)
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lpthread"]
+    cmd = [nvcc, "-shared"] + ARCH + ["-o", tmp] + objs + ["-lpthread", "-ldl"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout.decode(errors='replace')}")

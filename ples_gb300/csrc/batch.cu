@@ -41,6 +41,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "handle.h"
 #include "mg_device.cuh"
 #include "outer_device.cuh"
@@ -770,6 +772,10 @@ void to_stats(const InstState& S, ples_mg_stats* o) {
 
 int batch_solve(ples_mg_batch* b, double* const* fi, const double* const* rhs, double rel_tol, double abs_tol,
                 int max_cycles, ples_mg_stats* stats, bool device_ptrs) {
+    nvtxRangePushA("ples_mg batch solve");
+    struct Pop {
+        ~Pop() { nvtxRangePop(); }
+    } pop;
     const int nm = (int)b->mem.size();
     auto t0 = std::chrono::steady_clock::now();
     BK(cudaSetDevice(b->dev));

@@ -23,6 +23,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "line_tma.cuh"
 #include "handle.h"
 #include "mg_device.cuh"
@@ -633,8 +635,29 @@ void wall_fill(ples_mg_handle* h, double* p, const double* const cs[6], double a
 
 dim3 box_grid(const Geom& g) { return dim3((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2); }
 
+// NVTX ranges over the phases of a call (shown by Nsight Systems; without a
+// tool attached they cost a branch)
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+struct NvtxSpan {  // a range opened and closed at run time, closed at scope exit
+    bool open = false;
+    void begin(const char* name) {
+        end();
+        nvtxRangePushA(name);
+        open = true;
+    }
+    void end() {
+        if (open) nvtxRangePop();
+        open = false;
+    }
+    ~NvtxSpan() { end(); }
+};
+
 template <typename T>
 int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles, ples_mg_stats* st) {
+    NvtxRange range("ples_mg solve");
     LevelData& F = h->L[0];
     const Geom& g = F.g;
     // cells in the system: all interior cells, or the fluid ones of a mask
@@ -758,10 +781,13 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     }
     double rel = 0.0, rmax = 0.0, rel0 = -1.0;
     int it = 0, status = PLES_MG_NOT_CONVERGED, vcyc = 0;
+    NvtxSpan span;
+    span.begin("first residual");
     enqueue_residual(true);
     CK(cudaGetLastError());
     for (;;) {
         CK(cudaStreamSynchronize(h->st));
+        span.end();
         timed_collect(h);
         const double r2[2] = {h->h_red[0], h->h_red[1]};
         int flag = 0;
@@ -782,6 +808,7 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         if (it >= max_cycles) break;
         // inner solve of L e = r: V-cycles from e = 0 (F.rh holds r; the
         // residual kernel wrote it with a consistent ghost shell of zeros)
+        span.begin("outer iteration");
         if (graphs) {
             CK(cudaGraphLaunch(h->iter_exec, h->st));
             h->launches += h->iter_launches;
@@ -1170,6 +1197,7 @@ void mask_coef(ples_mg_handle* h, int lev, Coef<T>& c) {
 constexpr int kDenseMax = 3072;
 
 int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
+    NvtxRange range("ples_mg create");
     int rc = validate(d, h);
     if (rc) return rc;
     h->d = *d;
@@ -1939,6 +1967,7 @@ __global__ void k_contra(Geom g, Normals nrm, const double* __restrict__ u, cons
 // contravariant ones, of which the wall faces of vc are read).
 int project_core(ples_mg_handle* h, double* uc, double* vc, double* wc, double* u, double* v, double* w, double* fi,
                  double rel_tol, int max_cycles, ples_mg_stats* stats, bool with_contra) {
+    NvtxRange range(with_contra ? "ples_mg step" : "ples_mg project");
     auto t0 = std::chrono::steady_clock::now();
     const Geom& g = h->L[0].g;
     const size_t nuc = (size_t)(g.nx + 1) * g.ny * g.nz, nvc = (size_t)g.nx * (g.ny + 1) * g.nz,
@@ -2089,6 +2118,7 @@ int ples_mg_set_line_threads(ples_mg_handle* h, int level, int threads) {
 // ||r||/||b|| <= 1e-10 from zero).  The fastest setting is kept in the handle.
 int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) {
     if (!h || !out) return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    NvtxRange range("ples_mg autotune");
     return with_device(h, [&]() -> int {
         const Geom& g = h->L[0].g;
         const size_t nrh = (size_t)g.nx * g.ny * g.nz;
