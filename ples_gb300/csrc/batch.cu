@@ -74,7 +74,7 @@ struct AddTask { TaskHead h; Geom g; double* a; int box; int use_mean; };
 struct WallCTask { TaskHead h; Geom g; Coef<double> c; const double* p; double* w; };
 struct WallSTask { TaskHead h; Geom g; double* p; const double* w; };
 struct RoutTask { TaskHead h; Geom g; Coef<double> c; const double* x; const double* b; float* rin; double* psq; double* pmax; };
-struct LineTask { TaskHead h; Geom g; Coef<float> c; const float* cp; const float* pin; const float* pk; float* pout; const float* rh; float omega; int kpar; int zk; };
+struct LineTask { TaskHead h; Geom g; Coef<float> c; const float* cp; const float* pin; const float* pk; float* pout; const float* rh; float omega; int kpar; int zk; int wide; };
 struct RRTask { TaskHead h; Geom gf, gc; Coef<float> c; const float* p; const float* rh; float* rhc; int rx, ry, rz; };
 struct DenseTask { TaskHead h; Geom g; const float* S; const float* rh; float* p; };
 struct ProlTask { TaskHead h; Geom gf, gc; float* pf; const float* pc; int ry, rz; };
@@ -154,6 +154,17 @@ template <class T, bool ZIN>
 __global__ void __launch_bounds__(256, 3) kb_line(WALK_ARGS) {
     walk(t, n, total, ctr, st, ph, [](const LineTask& k, const Blk& B) {
         k_line_relax_blk<float, true, ZIN>(k.g, k.c, k.cp, k.pin, k.pk, k.pout, k.rh, k.omega, k.kpar, k.zk, B);
+    });
+}
+// a sweep step with 64-line tiles: 16 warps per CTA; the tasks of members
+// whose level does not take them run the 32-line body with the same warps
+template <class T, bool ZIN>
+__global__ void __launch_bounds__(512, 2) kb_line_wide(WALK_ARGS) {
+    walk(t, n, total, ctr, st, ph, [](const LineTask& k, const Blk& B) {
+        if (k.wide)
+            k_line_relax_x2_blk<ZIN>(k.g, k.c, k.cp, k.pin, k.pk, k.pout, k.rh, k.omega, k.kpar, k.zk, B);
+        else
+            k_line_relax_blk<float, true, ZIN>(k.g, k.c, k.cp, k.pin, k.pk, k.pout, k.rh, k.omega, k.kpar, k.zk, B);
     });
 }
 template <class T>
@@ -250,6 +261,7 @@ struct Step {
     int ntask = 0, total = 0;
     size_t off = 0;    // byte offset of the task array in the table buffer
     int threads = 0;   // CTA width of a smoother step (the tuned width of its largest grid)
+    bool wide = false; // a smoother step with 64-line tiles (kb_line_wide, 512 threads)
 };
 
 }  // namespace
@@ -266,7 +278,7 @@ struct ples_mg_batch {
     unsigned char* d_tab = nullptr;
     std::vector<unsigned char> tab;
     std::vector<Step> steps;
-    size_t smem_line = 0, smem_dense = 0;
+    size_t smem_line = 0, smem_dense = 0, smem_wide = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::string err;
@@ -332,6 +344,15 @@ dim3 rout_grid(const Geom& g) { return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g
 int build_steps(ples_mg_batch* b) {
     const int nm = (int)b->mem.size();
     Builder B{b};
+    // kb_line_wide runs the 64-line form or the 32-line form with 16 warps:
+    // its shared memory is the larger of the two over all members' levels
+    for (int i = 0; i < nm; ++i)
+        for (int n = 0; n < b->mem[i]->nlev; ++n) {
+            const size_t ny2 = (size_t)b->mem[i]->L[n].g.ny + 2;
+            b->smem_wide = std::max(b->smem_wide, std::max(3 * ny2 * 64 + 4 * 16 * 32, (3 * ny2 + 4 * 16) * 32) *
+                                                      sizeof(float));
+        }
+    const bool allow_wide = b->smem_wide <= 227 * 1024;
     // buffer roles per member and level: 0 -> (p, p2), 1 -> (p2, p)
     std::vector<std::vector<int>> cur(nm);
     int lmax = 0, numax = 0, inmax = 0, wmax = 0;
@@ -418,7 +439,10 @@ int build_steps(ples_mg_batch* b) {
                 t.omega = (float)h->omega;
                 t.kpar = par;
                 t.zk = (zin && par == 0) ? 1 : 0;
-                B.add(t, line_grid(L.g));
+                // 64-line tiles where they apply and fill at least one tile
+                t.wide = allow_wide && L.x2_ok && L.g.nx >= 64 ? 1 : 0;
+                B.add(t, t.wide ? dim3((L.g.nx + 63) / 64, (L.g.nz + 1) / 2, 1) : line_grid(L.g));
+                if (t.wide) B.cur.wide = true;
                 const long long cells = (long long)L.g.nx * L.g.ny * L.g.nz;
                 if (cells > big) {
                     big = cells;
@@ -624,10 +648,12 @@ int record_steps(ples_mg_batch* b) {
             case K_WALLS: rc = launch_step<WallSTask>(b, s, i, kb_walls<WallSTask>, b2, 0); break;
             case K_ROUT: rc = launch_step<RoutTask>(b, s, i, kb_rout<RoutTask>, b1, 0); break;
             case K_LINE0:
-                rc = launch_step<LineTask>(b, s, i, kb_line<LineTask, false>, dim3(s.threads), b->smem_line);
+                rc = s.wide ? launch_step<LineTask>(b, s, i, kb_line_wide<LineTask, false>, dim3(512), b->smem_wide)
+                            : launch_step<LineTask>(b, s, i, kb_line<LineTask, false>, dim3(s.threads), b->smem_line);
                 break;
             case K_LINE1:
-                rc = launch_step<LineTask>(b, s, i, kb_line<LineTask, true>, dim3(s.threads), b->smem_line);
+                rc = s.wide ? launch_step<LineTask>(b, s, i, kb_line_wide<LineTask, true>, dim3(512), b->smem_wide)
+                            : launch_step<LineTask>(b, s, i, kb_line<LineTask, true>, dim3(s.threads), b->smem_line);
                 break;
             case K_RR: rc = launch_step<RRTask>(b, s, i, kb_rr<RRTask>, b2, 0); break;
             case K_DENSE: rc = launch_step<DenseTask>(b, s, i, kb_dense<DenseTask>, b1, b->smem_dense); break;
@@ -674,6 +700,14 @@ int batch_create(ples_mg_handle* const* members, int n, ples_mg_batch* b) {
     BK(cudaMemcpyAsync(b->d_tab, b->tab.data(), b->tab.size(), cudaMemcpyHostToDevice, b->st));
     if (b->smem_line > 227 * 1024 || b->smem_dense > 227 * 1024)
         return bfail(b, PLES_MG_BAD_ARG, "a member's lines are too long for shared memory");
+    for (auto& s : b->steps)  // (no step is wide when smem_wide does not fit)
+        if (s.wide) {
+            BK(cudaFuncSetAttribute(kb_line_wide<LineTask, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)b->smem_wide));
+            BK(cudaFuncSetAttribute(kb_line_wide<LineTask, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)b->smem_wide));
+            break;
+        }
     BK(cudaFuncSetAttribute(kb_line<LineTask, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem_line));
     BK(cudaFuncSetAttribute(kb_line<LineTask, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem_line));
     BK(cudaFuncSetAttribute(kb_dense<DenseTask>, cudaFuncAttributeMaxDynamicSharedMemorySize,

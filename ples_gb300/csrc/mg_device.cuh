@@ -924,12 +924,13 @@ __device__ __forceinline__ void store_pair(const Geom& g, float* p, int i, int j
     }
 }
 
-// Shared memory: 3 arrays [ny+2][64] and the segment maps [4][16][32].
+// Block coordinates: x the 64-line tile, y the plane of this k parity; 16
+// warps.  Shared memory: 3 arrays [ny+2][64] and the segment maps [4][16][32].
 template <bool ZIN>
-__global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c, const float* __restrict__ cpa,
-                                                          const float* __restrict__ pin, const float* __restrict__ pk,
-                                                          float* __restrict__ pout, const float* __restrict__ rh,
-                                                          float omega, int kpar, int zk) {
+__device__ __forceinline__ void k_line_relax_x2_blk(Geom g, Coef<float> c, const float* __restrict__ cpa,
+                                                    const float* __restrict__ pin, const float* __restrict__ pk,
+                                                    float* __restrict__ pout, const float* __restrict__ rh,
+                                                    float omega, int kpar, int zk, const Blk& B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nj = g.ny + 2;
     float* G = reinterpret_cast<float*>(smem_raw);
@@ -940,9 +941,9 @@ __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c,
     float* SU2 = SV + 16 * 32;
     float* SV2 = SU2 + 16 * 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int k = 2 * blockIdx.y + 1 + kpar;
+    const int k = 2 * B.y + 1 + kpar;
     if (k > g.nz) return;
-    const int i0 = blockIdx.x * 64 + 1;
+    const int i0 = B.x * 64 + 1;
     // phase 1: line L = 32 (w / 8) + lane of the tile, row segment w % 8 of 8
     const int L = 32 * (w >> 3) + lane;
     const int ib = i0 + L;
@@ -959,6 +960,13 @@ __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c,
     seg_thomas<float, 64>(G, AL, CP, nj, io <= g.nx, SU, SV, lane, SU2, SV2);
     if (io <= g.nx)
         for (int j = w; j < nj; j += 16) store_pair(g, pout, io, j, k, G[j * 64 + lane], G[j * 64 + 32 + lane]);
+}
+template <bool ZIN>
+__global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c, const float* __restrict__ cpa,
+                                                          const float* __restrict__ pin, const float* __restrict__ pk,
+                                                          float* __restrict__ pout, const float* __restrict__ rh,
+                                                          float omega, int kpar, int zk) {
+    k_line_relax_x2_blk<ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
 }
 
 // ---------------------------------------------------------------------------
