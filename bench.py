@@ -49,6 +49,14 @@ REF_CYCLES_TO_1E10 = {"channel_256x128x256": 49, "channel_64x32x64": 17}
 # launches of the zebra smoother together): read p, rhs and the nine face
 # coefficients, write p (12 x 4 B)
 LINE_BYTES_PER_CELL = 48
+# the level-1 smoother of a workload and its DRAM bytes per sweep (read +
+# written, both k-parity launches) from one ncu capture:
+# profiles/line_relax_x2_channel_256x128x256.md
+LINE_TRAFFIC = {
+    "channel_256x128x256": (
+        "k_line_relax_x2<false> (zebra, 64-line tiles) level 1, one sweep = 2 launches (k parities)",
+        316386560 + 317648128),
+}
 
 
 def _peaks():
@@ -584,17 +592,8 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
     cells = w.cells
     avg_launch_s = kms / 1e3 / kn if kn else None
     achieved = LINE_BYTES_PER_CELL * cells / avg_launch_s / 1e9 if avg_launch_s else None
-    traffic = None
-    kernel = "eta-line smoother level 1, one sweep = 2 launches (k parities)"
-    prof = os.path.join(ROOT, "profiles", f"line_relax_{args.workload}.json")
-    if os.path.exists(prof):
-        try:
-            # per timed unit: one sweep = both k-parity launches
-            pj = json.load(open(prof))
-            traffic = pj.get("dram_bytes_per_sweep")
-            kernel = pj.get("kernel", kernel)
-        except Exception:
-            traffic = None
+    kernel, traffic = LINE_TRAFFIC.get(
+        args.workload, ("eta-line smoother level 1, one sweep = 2 launches (k parities)", None))
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
