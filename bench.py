@@ -39,24 +39,39 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Poisson solves/s to rel-resid 1e-10"
 UNIT = "solves/s"
-# V-cycles the reference algorithm (line SOR, omega 1.6, 5/10 sweeps, 4
-# levels) needs to reach ||r||/||b|| <= 1e-10 on these workloads, measured
-# with the CPU oracle to convergence (8 emulated ranks at 256x128x256: 49
-# cycles, 135 s; 1 rank at 64x32x64: 17 cycles); the CPU baseline times a
-# sample of cycles and scales by this count.
-REF_CYCLES_TO_1E10 = {"channel_256x128x256": 49, "channel_64x32x64": 17}
 # algorithmic bytes per cell of one FP32 eta-line sweep (both k-parity
 # launches of the zebra smoother together): read p, rhs and the nine face
 # coefficients, write p (12 x 4 B)
 LINE_BYTES_PER_CELL = 48
-# the level-1 smoother of a workload and its DRAM bytes per sweep (read +
-# written, both k-parity launches) from one ncu capture:
-# profiles/line_relax_x2_channel_256x128x256.md
+# DRAM bytes (read + written) of one level-1 sweep of the smoother, from one
+# ncu capture of `python bench.py --steps 1 --warmup 3 --fp64-steps 0
+# --e2e-steps 0 --no-cpu-baseline --batch-steps 0 --serve-requests 0
+# --ib-steps 0` with dram__bytes_read.sum + dram__bytes_write.sum over the
+# launches of one sweep; keyed by workload and the kernel that capture timed,
+# and reported only when the bench times that same kernel
 LINE_TRAFFIC = {
-    "channel_256x128x256": (
-        "k_line_relax_x2<false> (zebra, 64-line tiles) level 1, one sweep = 2 launches (k parities)",
-        316386560 + 317648128),
+    ("channel_256x128x256", "k_line_relax_x2"): 316386560 + 317648128,
 }
+# the level-1 smoother form (threads per CTA as ples_mg_set_line_threads
+# takes them) -> the kernel it launches
+LINE_KERNELS = {1024: "k_line_relax_x2", 512: "k_line_relax_w", 256: "k_line_relax", 128: "k_line_relax"}
+
+
+def _workload_config(w):
+    """The keys that define a workload, shared by both arms' `config`."""
+    return {"workload": w.name, "grid": f"{w.jx}x{w.jy}x{w.jz}", "cells": w.cells,
+            "wall_amplitude": w.amp, "y_stretch": w.beta, "rhs_seed": w.seed,
+            "tolerance": "||r||2/||b||2 <= 1e-10", "data": "seeded synthetic grid and RHS",
+            "l2": "inputs larger than L2 (no flush)"}
+
+
+def _ranks_for(w, cores):
+    """Emulated MPI ranks of the reference solver: the most threads up to
+    `cores` that divide jz at every one of its 4 levels (jz / 8)."""
+    for p in range(cores, 0, -1):
+        if (w.jz // 8) % p == 0:
+            return p
+    return 1
 
 
 def _peaks():
@@ -142,11 +157,11 @@ def replica_throughput(t_local, steps, world_size, dist=None, device="cpu"):
     return t, steps * world_size / t
 
 
-def cpu_baseline(workload, threads_cap=None, cycles=1):
+def cpu_baseline(workload, threads_cap=None):
     """Reference algorithm on the host: the CPU oracle (line SOR as in the
     reference's islor=1 option, 4 levels, kss 5/10, omega 1.6) with nproc
-    emulated MPI ranks as threads, timed over `cycles` V-cycles at the full
-    size and scaled to solves/s with the measured cycle count."""
+    emulated MPI ranks as threads, one complete solve from zero to
+    ||r||/||b|| <= 1e-10 on the full grid, timed whole (no extrapolation)."""
     from oracle.oracle import Oracle
     from ples_gb300 import synthetic as S
     w = S.WORKLOADS[workload]
@@ -155,26 +170,26 @@ def cpu_baseline(workload, threads_cap=None, cycles=1):
     cores = os.cpu_count() or 1
     if threads_cap:
         cores = min(cores, threads_cap)
-    # ranks must divide jz at every one of the 4 levels
-    nproc = 1
-    for p in range(cores, 0, -1):
-        if (w.jz // 8) % p == 0:
-            nproc = p
-            break
+    nproc = _ranks_for(w, cores)
     o = Oracle(x, y, z, islor=1, nproc=nproc)
     t0 = time.perf_counter()
-    _, cyc, _, rr = o.multi(rhs, eps=1e-30, ficycle=cycles)
-    dt = (time.perf_counter() - t0) / cycles
-    ncyc = REF_CYCLES_TO_1E10.get(workload)
-    value = 1.0 / (dt * ncyc) if ncyc else None
-    return {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
-            "sample": (f"{cycles} V-cycle(s) of the restated reference solver (line SOR, "
-                       f"{nproc} emulated MPI ranks as threads) on the full {workload} grid: "
-                       f"{dt:.2f} s per V-cycle x {ncyc} V-cycles to 1e-10"),
-            "seconds_per_vcycle": dt}
+    _, cyc, _, rr = o.multi(rhs, eps=1e-10, ficycle=400)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": UNIT, "cores": nproc, "kind": "port",
+            "sample": (f"one complete solve of the restated reference solver (line SOR, {nproc} emulated "
+                       f"MPI ranks as threads) on the full {workload} grid from zero to "
+                       f"||r||/||b|| = {rr:.2e}: {cyc} V-cycles in {dt:.1f} s"),
+            "vcycles": cyc, "seconds_per_solve": dt}
 
 
 def run_reference(args):
+    """The reference arm: the restated reference solver on the host cores
+    (the Fortran+MPI reference cannot be built on either machine).  One
+    complete solve from zero counts the V-cycles it needs to reach
+    ||r||/||b|| <= 1e-10 with this run's rank count; then each of the
+    warm-up and timed steps is one V-cycle of the same solve, and
+    value = 1 / (mean timed V-cycle x that count).  ms_per_step is the timed
+    step (one V-cycle)."""
     ws, rank, local = _dist()
     if rank != 0:
         return
@@ -184,14 +199,11 @@ def run_reference(args):
     w = S.WORKLOADS[args.workload]
     x, y, z = w.grid()
     rhs = w.rhs()
-    cores = os.cpu_count() or 1
-    nproc = 1
-    for p in range(cores, 0, -1):
-        if (w.jz // 8) % p == 0:
-            nproc = p
-            break
+    nproc = _ranks_for(w, os.cpu_count() or 1)
     o = Oracle(x, y, z, islor=1, nproc=nproc)
-    ncyc = REF_CYCLES_TO_1E10.get(args.workload)
+    t0 = time.perf_counter()
+    _, ncyc, _, rr = o.multi(rhs, eps=1e-10, ficycle=400)
+    t_solve = time.perf_counter() - t0
     times = []
     for s in range(warm + steps):
         t0 = time.perf_counter()
@@ -199,17 +211,21 @@ def run_reference(args):
         if s >= warm:
             times.append(time.perf_counter() - t0)
     t_cycle = sum(times) / len(times)
-    value = 1.0 / (t_cycle * ncyc) if ncyc else None
+    value = 1.0 / (t_cycle * ncyc)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-        "warmup": warm, "ms_per_step": t_cycle * ncyc * 1e3 if ncyc else None,
+        "warmup": warm, "ms_per_step": t_cycle * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": args.workload, "grid": f"{w.jx}x{w.jy}x{w.jz}", "cells": w.cells,
-                   "solver": "restated reference multi: line SOR (islor=1), omega 1.6, kss 5/10, 4 levels",
-                   "step": "one V-cycle per step, scaled by the V-cycles to 1e-10"},
+        "config": _workload_config(w),
+        "solver": {"kind": "restated reference multi: line SOR (islor=1), omega 1.6, kss 5/10, 4 levels, "
+                           f"{nproc} emulated MPI ranks as threads",
+                   "step": "one V-cycle; value = 1 / (ms_per_step x vcycles_to_tolerance)",
+                   "vcycles_to_tolerance": ncyc, "rel_residual_reached": rr,
+                   "full_solve_seconds": t_solve},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "port",
-                         "sample": f"1 V-cycle per step, {nproc} emulated ranks, x {ncyc} V-cycles"},
+                         "sample": (f"{steps} timed V-cycles ({t_cycle:.2f} s each) x {ncyc} V-cycles to 1e-10 "
+                                    f"counted in this run by one complete solve ({t_solve:.1f} s)")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -592,8 +608,9 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
     cells = w.cells
     avg_launch_s = kms / 1e3 / kn if kn else None
     achieved = LINE_BYTES_PER_CELL * cells / avg_launch_s / 1e9 if avg_launch_s else None
-    kernel, traffic = LINE_TRAFFIC.get(
-        args.workload, ("eta-line smoother level 1, one sweep = 2 launches (k parities)", None))
+    kname = LINE_KERNELS.get(m.line_threads(1), "eta-line smoother")
+    kernel = f"{kname} level 1, one sweep (its k-parity launches together)"
+    traffic = LINE_TRAFFIC.get((args.workload, kname))
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload)
@@ -602,11 +619,9 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded wavy-wall channel grid and divergence RHS)",
-        "config": {"workload": args.workload, "grid": f"{w.jx}x{w.jy}x{w.jz}", "cells": cells,
-                   "wall_amplitude": w.amp, "y_stretch": w.beta, "rhs_seed": w.seed,
-                   "precision": "mixed: FP32 V-cycle, FP64 residual/update/projection",
-                   "tolerance": "||r||2/||b||2 <= 1e-10", "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (no flush)", "levels": m.nlevel,
+        "config": _workload_config(w),
+        "solver": {"precision": "mixed: FP32 V-cycle, FP64 residual/update/projection",
+                   "parallelism": f"replicas x{ws}", "levels": m.nlevel,
                    "outer_iterations_mean": outer, "max_rel_residual": relres},
         "fp64": {"value": 1.0 / t64 if t64 else None, "unit": UNIT,
                  "ms_per_solve": t64 * 1e3 if t64 else None, "outer_iterations": st64["outer_iterations"]},

@@ -241,6 +241,10 @@ int ples_mg_autotune(ples_mg_handle *h, const double *rhs, ples_mg_tuning *out);
  * for another value, a form that does not apply at that level or whose
  * shared memory does not fit. */
 int ples_mg_set_line_threads(ples_mg_handle *h, int level, int threads);
+/* The form of the eta-line smoother at one level (1-based) as
+ * ples_mg_set_line_threads takes it: the default or the autotuner's
+ * choice.  No counterpart in the reference. */
+int ples_mg_get_line_threads(const ples_mg_handle *h, int level, int *threads);
 
 /* ---- many grids at once ------------------------------------------------
  * No counterpart in the reference, which solves one grid per run.  A batch
@@ -302,15 +306,19 @@ void ples_srv_destroy(ples_srv *s);
  *
  * On the fine level: r = L(fi) - rhs as in ples_mg_apply_residual with
  * level 1 and FP64 (resid_sndrcv.f03:2-156), and norms[0] = sum of r^2,
- * norms[1] = max |r| (the stop test of multi, multigrid.f03:595-631).
+ * norms[1] = max |r| (the stop test of multi, multigrid.f03:595-631).  With
+ * the descriptor's tipo, norms[1] runs over the fluid cells (tipo >= 2), as
+ * that stop test with bodyforce = 1 (multigrid.f03:615-631) and the solve's
+ * max_residual; with the descriptor's solid mask, solid cells are rows
+ * removed from the system: r = 0 there.
  * d_fi (0:jx+1,0:jy+1,0:jz+1) and d_rhs (1:jx,1:jy,1:jz) are device
  * buffers; the ghost layer of d_fi is used as given.  d_r (1:jx,1:jy,1:jz,
  * device) receives r, or is NULL.  norms is host memory; the call returns
  * after the result reached it.  stream NULL = the handle's stream.
- * The first call on each device looks the scratch address up
- * (cudaGetSymbolAddress, which may load the module), so make that first call
- * before any stream capture.  All calls on one device share the scratch:
- * calls that overlap in time on that device race; serialise them. */
+ * The scratch's device address is looked up (cudaGetSymbolAddress) when
+ * the handle is created, on the handle's device.  All calls on one device
+ * share the scratch: calls that overlap in time on that device race;
+ * serialise them. */
 int ples_mg_residual_norms_device(ples_mg_handle *h, const double *d_fi,
                                   const double *d_rhs, double *d_r, void *stream,
                                   double norms[2]);

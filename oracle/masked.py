@@ -203,3 +203,73 @@ def solve(orc, rhs, solid=None):
     p = x[qi]
     p = np.where(fluid, p - p[fluid].mean(), 0.0)
     return p
+
+
+def residual(orc, fi, rhs, solid=None):
+    """Masked fine-level residual of a field, vectorised for full-size grids:
+    returns (r, rw) with r = L(fi) - b on the interior cells (nx, ny, nz),
+    b the fluid-compatible right-hand side of solve() (zero on solid cells,
+    where r is zero too), and rw (nx, 2, nz) the residuals of the
+    homogeneous wall relations of the bottom (j = 0) and top (j = ny+1)
+    ghost rows (zero on rows next to solid cells).  fi (nx+2, ny+2, nz+2)
+    holds the field with its ghost layer as a solver returned it; its x/z
+    ghost shell is replaced by the periodic images first."""
+    nx, ny, nz = orc.dims(1)
+    solid = np.zeros((nx, ny, nz), dtype=bool) if solid is None else np.asarray(solid, dtype=bool)
+    m = mask_box(solid, nx, ny, nz)
+    c = apply_mask(_coef_boxes(orc, nx, ny, nz), m)
+    p = np.array(fi, dtype=np.float64, order="F", copy=True)
+    p[0] = p[nx]
+    p[nx + 1] = p[1]
+    p[:, :, 0] = p[:, :, nz]
+    p[:, :, nz + 1] = p[:, :, 1]
+    I, J, K = slice(1, nx + 1), slice(1, ny + 1), slice(1, nz + 1)
+
+    def P(di, dj, dk, i=I, j=J, k=K):
+        return p[i.start + di:i.stop + di, j.start + dj:j.stop + dj, k.start + dk:k.stop + dk]
+
+    def C(key, di, dj, dk):
+        return c[key][1 + di:nx + 1 + di, 1 + dj:ny + 1 + dj, 1 + dk:nz + 1 + dk]
+
+    # face fluxes at the high side of each interior cell (o = 0) and the low
+    # side (o = -1 along the face normal), the bracketed terms of
+    # resid_sndrcv.f03:85-147 with the scaled coefficients
+    def fx(o):
+        return (C("a1", o, 0, 0) * (P(o + 1, 0, 0) - P(o, 0, 0))
+                + C("b12", o, 0, 0) * (P(o + 1, 1, 0) + P(o, 1, 0) - P(o + 1, -1, 0) - P(o, -1, 0))
+                + C("b13", o, 0, 0) * (P(o + 1, 0, 1) + P(o, 0, 1) - P(o + 1, 0, -1) - P(o, 0, -1)))
+
+    def fy(o):
+        return (C("a2", 0, o, 0) * (P(0, o + 1, 0) - P(0, o, 0))
+                + C("b21", 0, o, 0) * (P(1, o + 1, 0) + P(1, o, 0) - P(-1, o + 1, 0) - P(-1, o, 0))
+                + C("b23", 0, o, 0) * (P(0, o + 1, 1) + P(0, o, 1) - P(0, o + 1, -1) - P(0, o, -1)))
+
+    def fz(o):
+        return (C("a3", 0, 0, o) * (P(0, 0, o + 1) - P(0, 0, o))
+                + C("b31", 0, 0, o) * (P(1, 0, o + 1) + P(1, 0, o) - P(-1, 0, o + 1) - P(-1, 0, o))
+                + C("b32", 0, 0, o) * (P(0, 1, o + 1) + P(0, 1, o) - P(0, -1, o + 1) - P(0, -1, o)))
+
+    r = fx(0)
+    r -= fx(-1)
+    r += fy(0)
+    r -= fy(-1)
+    r += fz(0)
+    r -= fz(-1)
+    fluid = ~solid
+    b = np.where(fluid, rhs, 0.0)
+    b = np.where(fluid, b - b[fluid].mean(), 0.0)
+    r -= b
+    r[solid] = 0.0
+    # wall rows: the flux through the wall face (faces 0 and ny) vanishes
+    rw = np.zeros((nx, 2, nz))
+    for s, (jf, jl) in enumerate(((0, 0), (ny, ny))):
+        a2 = c["a2"][I, jf, K]
+        b21 = c["b21"][I, jf, K]
+        b23 = c["b23"][I, jf, K]
+
+        def Q(di, dj, dk):
+            return p[1 + di:nx + 1 + di, jl + dj, 1 + dk:nz + 1 + dk]
+
+        rw[:, s, :] = (a2 * (Q(0, 1, 0) - Q(0, 0, 0)) + b21 * (Q(1, 1, 0) + Q(1, 0, 0) - Q(-1, 1, 0) - Q(-1, 0, 0))
+                       + b23 * (Q(0, 1, 1) + Q(0, 0, 1) - Q(0, 1, -1) - Q(0, 0, -1)))
+    return r, rw

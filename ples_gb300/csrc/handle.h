@@ -57,6 +57,7 @@ struct ples_mg_handle {
     double* red = nullptr;                               // 2 doubles on the device (+ dflag)
     int* dflag = nullptr;                                // bounded-wait error flag, inside red
     double* h_red = nullptr;                             // pinned host copy
+    double* norm_scratch = nullptr;  // device address of the library's fixed residual scratch (this device)
     double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging
     uint8_t* tipo = nullptr;  // level-1 cell types (0 solid, 1 IB, 2 fluid, 3 other), or null
     double* cs_c[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // this call's wall fluxes

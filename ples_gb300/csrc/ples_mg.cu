@@ -1196,6 +1196,8 @@ void mask_coef(ples_mg_handle* h, int lev, Coef<T>& c) {
 // included): coarsening stops at the first level at or below it
 constexpr int kDenseMax = 3072;
 
+int lookup_norm_scratch(ples_mg_handle* h);
+
 int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     NvtxRange range("ples_mg create");
     int rc = validate(d, h);
@@ -1403,7 +1405,8 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     }
     // walled x / z: their ghosts and edges couple to the y-wall rows
     if (h->walls_xz) h->wall_passes = std::max(h->wall_passes, 30);
-    return PLES_MG_OK;
+    // the device address of the fixed scratch of ples_mg_residual_norms_device
+    return lookup_norm_scratch(h);
 }
 
 int upload_cs(ples_mg_handle* h, const double* const cs[6], bool device_ptrs) {
@@ -2111,6 +2114,13 @@ int ples_mg_set_line_threads(ples_mg_handle* h, int level, int threads) {
     return PLES_MG_OK;
 }
 
+int ples_mg_get_line_threads(const ples_mg_handle* h, int level, int* threads) {
+    if (!h || !threads) return PLES_MG_BAD_ARG;
+    if (level < 1 || level > h->nlev) return PLES_MG_BAD_ARG;
+    *threads = h->L[level - 1].line_threads;
+    return PLES_MG_OK;
+}
+
 // Autotuner: first the form of the eta-line smoother per level (128, 256 or
 // 512 threads on 32-line tiles, 1024 for the 64-line tiles; the kernel's own
 // time, CUDA events), then the sweep count per
@@ -2248,7 +2258,6 @@ namespace {
 
 constexpr int kNormMaxBlocks = 65536;
 constexpr int kNormKC = 8;
-constexpr int kNormMaxDevices = 64;
 static __device__ __align__(256) double g_norm_scratch[2 * kNormMaxBlocks + 2];
 
 // the caller's fi (0:jx+1,0:jy+1,0:jz+1), column-major
@@ -2281,12 +2290,18 @@ __device__ __forceinline__ double cflux_z(const Coef<double>& c, long long q, co
 // read straight from the caller's arrays, with the flux sharing of
 // k_resid_outer2; optional r output in the (1:jx,1:jy,1:jz) layout and
 // per-block partials into part[blk] (sum of squares), part[maxoff + blk]
-// (max |r|).  The ghost layer of fi is used as the caller left it.
+// (max |r|).  The ghost layer of fi is used as the caller left it.  solid
+// (level-1 byte box, 1 = solid, or null): those cells are rows removed from
+// the system, r = 0.  tipo (level-1 byte box or null): the max runs over
+// the fluid cells only, as multi's stop test with bodyforce = 1
+// (multigrid.f03:615-631) and the solver's own outer residual; the sum of
+// squares runs over every cell, as the solver's.
 template <int KC>
 __global__ void __launch_bounds__(256) k_resid_norm_compact(Geom g, Coef<double> c, CompactP P,
                                                             const double* __restrict__ rhs,
                                                             double* __restrict__ rout, double* __restrict__ part,
-                                                            long long maxoff) {
+                                                            long long maxoff, const uint8_t* __restrict__ solid,
+                                                            const uint8_t* __restrict__ tipo) {
     __shared__ double sN[8][32];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i = blockIdx.x * 32 + tx + 1, j = blockIdx.y * 8 + ty + 1;
@@ -2309,10 +2324,11 @@ __global__ void __launch_bounds__(256) k_resid_norm_compact(Geom g, Coef<double>
         const double fF = cflux_z(c, q, P, qp);
         if (act) {
             const long long qr = (i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
-            const double r = ((fE - fW) + (fN - fS) + (fF - fB)) - rhs[qr];
+            // a solid cell of an immersed-boundary mask is a removed row: r = 0
+            const double r = solid && solid[q] ? 0.0 : ((fE - fW) + (fN - fS) + (fF - fB)) - rhs[qr];
             if (rout) rout[qr] = r;
             s += r * r;
-            m = fmax(m, fabs(r));
+            if (!tipo || tipo[q] == 2) m = fmax(m, fabs(r));  // the stop test's max: fluid cells (tipo >= 2)
         }
         fB = fF;
     }
@@ -2324,25 +2340,16 @@ __global__ void __launch_bounds__(256) k_resid_norm_compact(Geom g, Coef<double>
     }
 }
 
-// Device address of g_norm_scratch on the handle's device (current when this
-// runs).  The first call on each device looks it up with
-// cudaGetSymbolAddress, which may load the module on that device; later
-// calls reuse the cached address.
-int norm_scratch(ples_mg_handle* h, double** out) {
-    static std::mutex mu;
-    static double* addr[kNormMaxDevices] = {};
-    if (h->dev < 0 || h->dev >= kNormMaxDevices)
-        return fail(h, PLES_MG_BAD_ARG, "device %d: the residual scratch serves devices 0..%d", h->dev,
-                    kNormMaxDevices - 1);
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[h->dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_norm_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(h, PLES_MG_CUDA_ERROR, "cudaGetSymbolAddress(residual scratch): %s", cudaGetErrorString(e));
-        addr[h->dev] = static_cast<double*>(p);
-    }
-    *out = addr[h->dev];
+// Device address of g_norm_scratch on the device that is current (the
+// handle's, during ples_mg_create).  Host code holds only a stand-in for the
+// array's name, so kernels get this address, looked up once per handle when
+// it is created: it stays valid for the handle's life on its device.
+int lookup_norm_scratch(ples_mg_handle* h) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_norm_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(h, PLES_MG_CUDA_ERROR, "cudaGetSymbolAddress(residual scratch): %s", cudaGetErrorString(e));
+    h->norm_scratch = static_cast<double*>(p);
     return PLES_MG_OK;
 }
 
@@ -2359,12 +2366,12 @@ extern "C" int ples_mg_residual_norms_device(ples_mg_handle* h, const double* d_
             return fail(h, PLES_MG_BAD_ARG,
                         "grid %dx%dx%d needs %lld residual blocks; the static scratch holds %d (about 512^3 cells)",
                         g.nx, g.ny, g.nz, nblk, kNormMaxBlocks);
-        double* part = nullptr;
-        int rc = norm_scratch(h, &part);
-        if (rc) return rc;
+        double* part = h->norm_scratch;
+        if (!part) return fail(h, PLES_MG_CUDA_ERROR, "the residual scratch address was not set up");
         cudaStream_t st = stream ? (cudaStream_t)stream : h->st;
         const CompactP P{d_fi, g.nx + 2, (long long)(g.nx + 2) * (g.ny + 2)};
-        k_resid_norm_compact<kNormKC><<<grd, 256, 0, st>>>(g, h->L[0].cd, P, d_rhs, d_r, part, kNormMaxBlocks);
+        k_resid_norm_compact<kNormKC><<<grd, 256, 0, st>>>(g, h->L[0].cd, P, d_rhs, d_r, part, kNormMaxBlocks,
+                                                           h->masked ? h->mask[0] : nullptr, h->tipo);
         k_reduce_final<<<1, 1024, 0, st>>>(part, part + kNormMaxBlocks, nblk, part + 2 * kNormMaxBlocks);
         h->launches += 2;
         CK(cudaGetLastError());

@@ -71,7 +71,7 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
            "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune", "ples_mg_project",
            "ples_mg_step", "ples_mg_residual_norms_device", "ples_mg_read_grid", "ples_mg_potenziale_ibm",
-           "ples_mg_set_line_threads")
+           "ples_mg_set_line_threads", "ples_mg_get_line_threads")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -108,6 +108,7 @@ def load(build=True):
     L.ples_mg_residual_norms_device.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_double)]
     L.ples_mg_autotune.argtypes = [vp, vp, C.POINTER(Tuning)]
     L.ples_mg_set_line_threads.argtypes = [vp, C.c_int, C.c_int]
+    L.ples_mg_get_line_threads.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
     L.ples_mg_project.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_step.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_read_grid.argtypes = [C.c_char_p, vp, vp, vp, vp, vp]
@@ -346,6 +347,12 @@ class Multigrid:
         """Smoother form at one level (1-based): 128, 256 or 512 threads on
         32-line tiles, or 1024 for the 64-line tiles (ples_mg_set_line_threads)."""
         self._check(self._L.ples_mg_set_line_threads(self._h, level, threads))
+
+    def line_threads(self, level):
+        """The smoother form at one level (ples_mg_get_line_threads)."""
+        t = C.c_int()
+        self._check(self._L.ples_mg_get_line_threads(self._h, level, C.byref(t)))
+        return t.value
 
     # -- instrumentation ------------------------------------------------------
     def counters(self):
