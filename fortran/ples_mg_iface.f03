@@ -19,7 +19,9 @@ module ples_mg_iface
     use iso_c_binding
     implicit none
 
+    integer(c_int), parameter :: PLES_MG_ABI_VERSION = 5
     integer(c_int), parameter :: PLES_MG_OK = 0, PLES_MG_NOT_CONVERGED = 1
+    integer(c_int), parameter :: PLES_MG_SMOOTHER_LINE = 0, PLES_MG_SMOOTHER_POINT = 3
     integer(c_int), parameter :: PLES_MG_PREC_FP64 = 0, PLES_MG_PREC_MIXED = 1
     integer(c_int), parameter :: PLES_MG_COORDS_NODES = 0, PLES_MG_COORDS_GHOSTED8 = 1
 
@@ -40,6 +42,7 @@ module ples_mg_iface
         integer(c_int) :: coarsening
         type(c_ptr)    :: solid
         type(c_ptr)    :: tipo
+        integer(c_int) :: freesurface
     end type ples_mg_desc
 
     type, bind(C) :: ples_mg_stats
@@ -94,6 +97,20 @@ module ples_mg_iface
             type(c_ptr), value :: handle, fi
         end function ples_mg_potenziale_ibm
 
+        integer(c_int) function ples_mg_set_surface_pressure(handle, next_prs) &
+                bind(C, name="ples_mg_set_surface_pressure")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: handle, next_prs
+        end function ples_mg_set_surface_pressure
+
+        integer(c_int) function ples_mg_abi_layout(abi_version, desc_size, stats_size, desc_offsets, &
+                                                   stats_offsets) bind(C, name="ples_mg_abi_layout")
+            import :: c_int, c_long_long
+            integer(c_int), intent(out) :: abi_version
+            integer(c_long_long), intent(out) :: desc_size, stats_size
+            integer(c_long_long), intent(out) :: desc_offsets(24), stats_offsets(8)
+        end function ples_mg_abi_layout
+
         integer(c_int) function ples_mg_read_grid(path, lengths, dims, x, y, z) bind(C, name="ples_mg_read_grid")
             import :: c_int, c_ptr, c_char, c_double
             character(kind=c_char), dimension(*), intent(in) :: path
@@ -106,6 +123,38 @@ module ples_mg_iface
     type(c_ptr), save :: mg_handle = c_null_ptr
 
 contains
+
+    !-------------------------------------------------------------------
+    ! .true. when the bind(C) types above have the layout the library was
+    ! compiled with (size of each type and the byte offset of every field)
+    logical function ples_mg_layout_ok()
+        type(ples_mg_desc), target :: d
+        type(ples_mg_stats), target :: s
+        integer(c_int) :: ver
+        integer(c_long_long) :: dsize, ssize, doff(24), soff(8), mine_d(24), mine_s(8), base
+        integer :: stat
+        stat = ples_mg_abi_layout(ver, dsize, ssize, doff, soff)
+        base = transfer(c_loc(d), base)
+        mine_d = [transfer(c_loc(d%jx), base), transfer(c_loc(d%jy), base), transfer(c_loc(d%jz), base), &
+                  transfer(c_loc(d%ip), base), transfer(c_loc(d%jp), base), transfer(c_loc(d%kp), base), &
+                  transfer(c_loc(d%nlevmax), base), transfer(c_loc(d%omega), base), &
+                  transfer(c_loc(d%precision), base), transfer(c_loc(d%coords_layout), base), &
+                  transfer(c_loc(d%x), base), transfer(c_loc(d%y), base), transfer(c_loc(d%z), base), &
+                  transfer(c_loc(d%dt), base), transfer(c_loc(d%device), base), &
+                  transfer(c_loc(d%nu_pre), base), transfer(c_loc(d%nu_post), base), &
+                  transfer(c_loc(d%nu_coarse), base), transfer(c_loc(d%inner_cycles), base), &
+                  transfer(c_loc(d%smoother), base), transfer(c_loc(d%coarsening), base), &
+                  transfer(c_loc(d%solid), base), transfer(c_loc(d%tipo), base), &
+                  transfer(c_loc(d%freesurface), base)] - base
+        base = transfer(c_loc(s), base)
+        mine_s = [transfer(c_loc(s%outer_iterations), base), transfer(c_loc(s%vcycles), base), &
+                  transfer(c_loc(s%rel_residual), base), transfer(c_loc(s%max_residual), base), &
+                  transfer(c_loc(s%rhs_norm), base), transfer(c_loc(s%rhs_mean_removed), base), &
+                  transfer(c_loc(s%seconds), base), transfer(c_loc(s%status), base)] - base
+        ples_mg_layout_ok = stat == PLES_MG_OK .and. ver == PLES_MG_ABI_VERSION .and. &
+                            dsize == c_sizeof(d) .and. ssize == c_sizeof(s) .and. &
+                            all(doff == mine_d) .and. all(soff == mine_s)
+    end function ples_mg_layout_ok
 
     !-------------------------------------------------------------------
     ! after metrica: x, y, z are the ghosted node arrays of myarrays_metri3
@@ -122,7 +171,7 @@ contains
                          precision=precision, coords_layout=PLES_MG_COORDS_GHOSTED8, &
                          x=c_loc(x(-8, -8, -8)), y=c_loc(y(-8, -8, -8)), z=c_loc(z(-8, -8, -8)), &
                          dt=dt, device=0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0, &
-                         smoother=0, coarsening=0, solid=c_null_ptr, tipo=c_null_ptr)
+                         smoother=0, coarsening=0, solid=c_null_ptr, tipo=c_null_ptr, freesurface=0)
         if (c_associated(mg_handle)) call ples_mg_destroy(mg_handle)
         stat = ples_mg_create(d, mg_handle)
         if (stat /= PLES_MG_OK) error stop 'ples_mg_create failed'

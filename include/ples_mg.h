@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define PLES_MG_ABI_VERSION 4
+#define PLES_MG_ABI_VERSION 5
 
 /* status codes */
 enum {
@@ -63,8 +63,13 @@ typedef struct {
     int nu_coarse;         /* sweeps on the coarsest level (0 = default)            */
     int inner_cycles;      /* V-cycles per outer FP64 iteration (0 = default)       */
     int smoother;          /* 0 = zebra eta-line SOR (Gauss-Seidel in x and z as the
-                              reference's line SOR); 1 = eta-line Jacobi;
-                              2 = zebra with its rows staged by TMA (FP32) */
+                              reference's line SOR, islor = 1); 1 = eta-line Jacobi;
+                              2 = zebra with its rows staged by TMA (FP32);
+                              3 = multicolour point SOR, the reference's
+                              default islor = 0 (solut_sndrcv_sor,
+                              multigrid.f03:656-1010; omega default 1.0;
+                              periodic directions need even cell counts on
+                              every smoothed level) */
     int coarsening;        /* 0 = full, the reference's hierarchy (mul_met);
                               1 = semi-coarsening where x/z spacings differ     */
     const unsigned char *solid; /* immersed-boundary mask (1:jx,1:jy,1:jz), 1 =
@@ -80,6 +85,15 @@ typedef struct {
                               then runs over the fluid cells only; the operator
                               is unchanged.  Also the input of
                               ples_mg_potenziale_ibm.  Not for batches. */
+    int freesurface;       /* multi's freesurface argument (multigrid.f03:48): 1 =
+                              the top wall row takes the free-surface relation
+                              of mul_boun_sndrcv (multigrid.f03:1188-1222) with
+                              the surface pressure of
+                              ples_mg_set_surface_pressure; the pressure level
+                              is then fixed (no compatibility shift, no mean
+                              removal).  Needs smoother 3: the reference's line
+                              SOR keeps the wall relation (multigrid.f03:2019).
+                              Not for batches. */
 } ples_mg_desc;
 
 typedef struct {
@@ -94,6 +108,19 @@ typedef struct {
 } ples_mg_stats;
 
 typedef struct ples_mg_handle ples_mg_handle;
+
+/* Layout of the two structures above as this library was compiled: its
+ * PLES_MG_ABI_VERSION, sizeof(ples_mg_desc), sizeof(ples_mg_stats) and the
+ * byte offset of every field in declaration order (desc_offsets holds
+ * PLES_MG_DESC_FIELDS values, stats_offsets PLES_MG_STATS_FIELDS; any
+ * pointer may be NULL).  A binding compiled against its own copy of this
+ * header (C, Fortran bind(C) types, a ctypes mirror) compares them with
+ * its own to detect a stale copy.  No counterpart in the reference, whose
+ * multi exchanges module variables, not structures. */
+#define PLES_MG_DESC_FIELDS 24
+#define PLES_MG_STATS_FIELDS 8
+int ples_mg_abi_layout(int *abi_version, long long *desc_size, long long *stats_size,
+                       long long *desc_offsets, long long *stats_offsets);
 
 /* Build the coefficient hierarchy on the device and keep it resident.
  * Replaces metrica (fsrc/metrica.f03:2-501), cellep (fsrc/cellep.f03),
@@ -158,6 +185,15 @@ int ples_mg_apply_prolong(ples_mg_handle *h, int level, double *prf,
 /* kernels launched on the device by this handle so far, and its resident
  * device bytes */
 int ples_mg_counters(ples_mg_handle *h, long long *launches, long long *device_bytes);
+/* Polls a bounded device wait makes before it gives up (the mbarrier waits
+ * of the TMA-staged smoother, smoother 2, the only waits on the device; they
+ * also give up after 2 s): polls < 0 restores the default (2^26).  A wait
+ * that gives up makes the solve return PLES_MG_DEVICE_TIMEOUT, after its CTA
+ * has waited (with the default limits) for its copies still in flight; the
+ * handle stays usable.  For tests of that path: 0 makes every wait give up
+ * at once.  No counterpart in the reference. */
+int ples_mg_set_wait_limit(ples_mg_handle *h, long long polls);
+
 /* time one kernel kind at one level with CUDA events on the solve stream:
  * kind 0 eta-line smoother, 1 residual+restriction, 2 prolongation,
  * 3 FP64 outer residual; kind -1 switches timing off.  Resets the totals. */
@@ -241,6 +277,12 @@ int ples_mg_autotune(ples_mg_handle *h, const double *rhs, ples_mg_tuning *out);
  * for another value, a form that does not apply at that level or whose
  * shared memory does not fit. */
 int ples_mg_set_line_threads(ples_mg_handle *h, int level, int threads);
+/* The surface pressure PrS0 of a free-surface handle: next_prs (1:jx,1:jz)
+ * (myarrays_velo3, set by fsrc/contourp.f03:160), host, used by the
+ * following solves on level 1 (multigrid.f03:1207-1213); NULL = zero, as the
+ * reference's first time step (iterat = 1).  BAD_ARG without
+ * desc.freesurface. */
+int ples_mg_set_surface_pressure(ples_mg_handle *h, const double *next_prs);
 /* The form of the eta-line smoother at one level (1-based) as
  * ples_mg_set_line_threads takes it: the default or the autotuner's
  * choice.  No counterpart in the reference. */

@@ -49,6 +49,7 @@ def lib():
         L.orc_multi.argtypes = [C.c_void_p, _dp, _dp, C.c_void_p, C.c_double, C.c_int, C.c_int,
                                 C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_true_residual.argtypes = [C.c_void_p, _dp, _dp, C.c_void_p, _dp, C.c_int]
+        L.orc_set_free_surface.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _lib = L
     return _lib
 
@@ -84,6 +85,16 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+    def set_free_surface(self, on=True, next_prs=None):
+        """multi's freesurface argument and the surface pressure next_prs
+        (jx, jz) of level 1 (None: the first time step, PrS0 = 0)."""
+        self._prs = None if next_prs is None else _f(next_prs)
+        if self._prs is not None and self._prs.shape != (self.jx, self.jz):
+            raise ValueError("next_prs must be (jx, jz)")
+        ptr = None if self._prs is None else self._prs.ctypes.data
+        if lib().orc_set_free_surface(self._h, 1 if on else 0, ptr):
+            raise ValueError("bad free-surface setting")
 
     def dims(self, n):
         a, b, c = C.c_int(), C.c_int(), C.c_int()

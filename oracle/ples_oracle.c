@@ -63,6 +63,8 @@ struct orc_problem {
     int jx, jy, jz, ip, jp, kp, nproc, nlevel, islor;
     int jxc[MAXLEV + 1], jyc[MAXLEV + 1], jzc[MAXLEV + 1];
     double omega, dt;
+    int freesurface;  /* multi's freesurface argument (multigrid.f03:48) */
+    double *next_prs; /* surface pressure next_prs(1:jx,1:jz) of myarrays_velo3, or NULL */
     arr3 x, y, z;
     arr3 giac;
     orc_level lev[MAXLEV + 1];
@@ -571,7 +573,20 @@ void orc_destroy(orc_problem *p) {
         a3_free(&L->aa); a3_free(&L->bb); a3_free(&L->cc);
     }
     a3_free(&p->x); a3_free(&p->y); a3_free(&p->z); a3_free(&p->giac);
+    free(p->next_prs);
     free(p);
+}
+
+int orc_set_free_surface(orc_problem *p, int freesurface, const double *next_prs) {
+    if (!p || (freesurface != 0 && freesurface != 1)) return -1;
+    p->freesurface = freesurface;
+    free(p->next_prs);
+    p->next_prs = NULL;
+    if (next_prs) {
+        p->next_prs = (double *)malloc(sizeof(double) * (size_t)p->jx * p->jz);
+        memcpy(p->next_prs, next_prs, sizeof(double) * (size_t)p->jx * p->jz);
+    }
+    return 0;
 }
 
 int orc_nlevel(const orc_problem *p) { return p->nlevel; }
@@ -638,8 +653,9 @@ static double cs_at(const arr3 *a, int u, int v) {
     return a->d ? AT(*a, u, v, 0) : 0.0;
 }
 
-/* mul_boun_sndrcv, multigrid.f03:1013-1936 (freesurface = 0) */
-static void mul_boun(orc_rank *R, int n) {
+/* mul_boun_sndrcv, multigrid.f03:1013-1936.  fs: its freesurface argument
+ * (the point SOR passes multi's, the line SOR always 0, multigrid.f03:2019) */
+static void mul_boun(orc_rank *R, int n, int fs) {
     orc_world *W = R->W;
     orc_problem *P = W->P;
     orc_level *L = &P->lev[n];
@@ -685,9 +701,35 @@ static void mul_boun(orc_rank *R, int n) {
                     AT(*pr, nx + 1, j, k) = AT(*pr, 1, j, k);
                 }
         }
-        /* bottom and upper (:1160-1262), freesurface = 0 branch */
+        /* bottom and upper (:1160-1262) */
         for (int k = ks; k <= ke; k++)
             for (int i = 1; i <= nx; i++) {
+                if (fs) {
+                    /* free surface at the top (:1188-1222): PrS0 = 0 at the
+                     * first time step (next_prs not given) and on coarse
+                     * levels, next_prs(i,k) on level 1 otherwise; the
+                     * bottom keeps its wall relation */
+                    double inv_r22 = 1. / AT(*r22, i, 0, k);
+                    AT(*pr, i, 0, k) =
+                        AT(*pr, i, 1, k) - an * cs_at(&W->cs3, i, k) * inv_dt * inv_r22 +
+                        coef * inv_r22 *
+                            (AT(*r21, i, 0, k) * (AT(*pr, i + 1, 1, k) + AT(*pr, i + 1, 0, k) -
+                                                  AT(*pr, i - 1, 1, k) - AT(*pr, i - 1, 0, k)) +
+                             AT(*r23, i, 0, k) * (AT(*pr, i, 1, k + 1) + AT(*pr, i, 0, k + 1) -
+                                                  AT(*pr, i, 1, k - 1) - AT(*pr, i, 0, k - 1)));
+                    double prs0 = 0.;
+                    if (n == 1 && P->next_prs) prs0 = P->next_prs[(size_t)(k - 1) * P->jx + (i - 1)];
+                    inv_r22 = 1. / AT(*r22, i, ny, k);
+                    AT(*pr, i, ny + 1, k) =
+                        (prs0 * 2) -
+                        (AT(*pr, i, ny, k) -
+                         coef * inv_r22 *
+                             (AT(*r21, i, ny, k) * (AT(*pr, i + 1, ny + 1, k) + AT(*pr, i + 1, ny, k) -
+                                                    AT(*pr, i - 1, ny + 1, k) - AT(*pr, i - 1, ny, k)) +
+                              AT(*r23, i, ny, k) * (AT(*pr, i, ny + 1, k + 1) + AT(*pr, i, ny, k + 1) -
+                                                    AT(*pr, i, ny + 1, k - 1) - AT(*pr, i, ny, k - 1))));
+                    continue;
+                }
                 double inv_r22 = 1. / AT(*r22, i, 0, k);
                 AT(*pr, i, 0, k) =
                     AT(*pr, i, 1, k) - an * cs_at(&W->cs3, i, k) * inv_dt * inv_r22 +
@@ -925,7 +967,7 @@ static void smooth_sor(orc_rank *R, int n, int kss, const arr3 *rh) {
     arr3 *r21 = &G21(L), *r22 = &G22(L), *r23 = &G23(L);
     arr3 *r31 = &G31(L), *r32 = &G32(L), *r33 = &G33(L);
     for (int kk = 1; kk <= kss; kk++) {
-        mul_boun(R, n);
+        mul_boun(R, n, P->freesurface);
         if (P->kp == 0) zperiodic_planes(R, n);
         for (int k = ks; k <= ke; k++)
             for (int j = 1; j <= ny; j++) {
@@ -1018,7 +1060,7 @@ static void smooth_slor(orc_rank *R, int n, int kss, const arr3 *rh) {
     double *aa0 = malloc(sizeof(double) * (ny + 2)), *bb0 = malloc(sizeof(double) * (ny + 2));
     double *cc0 = malloc(sizeof(double) * (ny + 2)), *ff0 = malloc(sizeof(double) * (ny + 2));
     for (int kk = 1; kk <= kss; kk++) {
-        mul_boun(R, n);
+        mul_boun(R, n, 0); /* the line SOR sets freesurface = 0 (multigrid.f03:2019) */
         if (P->kp == 0) zperiodic_planes(R, n);
         for (int k = ks; k <= ke; k++) {
             if (P->ip == 0)
@@ -1422,7 +1464,7 @@ int orc_ghost_fill(orc_problem *p, int n, double *pr, const double *const cs[6])
     world_init(&W, p, 1, cs);
     arr3 *a = &W.ranks[0].pr[n];
     memcpy(a->d, pr, sizeof(double) * a3_size(a));
-    mul_boun(&W.ranks[0], n);
+    mul_boun(&W.ranks[0], n, p->freesurface);
     memcpy(pr, a->d, sizeof(double) * a3_size(a));
     world_free(&W);
     p->nproc = saved;

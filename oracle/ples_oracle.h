@@ -39,6 +39,15 @@ orc_problem *orc_create(int jx, int jy, int jz, int ip, int jp, int kp,
 void orc_destroy(orc_problem *p);
 const char *orc_last_error(void);
 
+/* multi's freesurface argument (multigrid.f03:48): 1 puts the free-surface
+ * relation of mul_boun_sndrcv (multigrid.f03:1188-1222) on the top ghost row
+ * of the point SOR's ghost fill (the line SOR keeps the wall relation, as the
+ * reference's sets freesurface = 0, multigrid.f03:2019) and of
+ * orc_ghost_fill.  next_prs (1:jx,1:jz): the surface pressure PrS0 of level
+ * 1 (myarrays_velo3 next_prs, set by contourp.f03:160), or NULL for the
+ * first time step, where the reference uses PrS0 = 0. */
+int orc_set_free_surface(orc_problem *p, int freesurface, const double *next_prs);
+
 int orc_nlevel(const orc_problem *p);
 /* jxc(n), jyc(n), jzc(n) for n=1..nlevel */
 void orc_level_dims(const orc_problem *p, int n, int *nx, int *ny, int *nz);

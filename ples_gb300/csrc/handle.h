@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "line_pair.cuh"
 #include "line_tma.cuh"
 #include "mg_device.cuh"
 #include "ples_mg.h"
@@ -26,14 +27,16 @@ struct LevelData {
     void* p2 = nullptr;
     void* rh = nullptr;
     void* cp = nullptr;          // LU factor c' of the eta-line operator (T box)
+    void* im = nullptr;          // pivot reciprocals 1/m of that operator (FP32 box, 64-line-tile levels)
     ples::Coef<float> cf{};             // FP32 scaled coefficients (mixed)
     ples::Coef<double> cd{};            // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
     bool has_cf = false, has_cd = false;
     // TMA-staged zebra smoother (FP32): tensor maps of this level's fields;
     // pA/pB are the buffers behind maps.pA/pB (p and p2 swap every sweep)
-    // CTA width of the eta-line smoother: 128, 256 or 512 threads on 32-line
-    // tiles, or 1024 for the 64-line-tile form (512 threads, k_line_relax_x2);
-    // autotuned
+    // form of the eta-line smoother: 128, 256 or 512 threads on 32-line
+    // tiles, 1024 for the 64-line-tile form (512 threads, k_line_relax_x2),
+    // 2048 for the 64-line tiles with the pair build (256 threads,
+    // k_line_relax_p2); autotuned
     int line_threads = 256;
     bool x2_ok = false;  // the 64-line-tile form applies (FP32, x and z periodic, nx even, nz >= 2)
     bool tma = false;
@@ -52,10 +55,13 @@ struct ples_mg_handle {
     double* wbuf = nullptr;                              // 2*nx*nz wall rows
     void* sbuf = nullptr;                                // ghosts of walled x/z directions (side_cells, 8 B each)
     bool walls_xz = false;                               // ip = 1 or kp = 1
+    bool fs = false;                                     // free surface at the top wall (desc.freesurface)
+    double* prs = nullptr;                               // its surface pressure PrS0 (1:jx,1:jz), device
     double *part_a = nullptr, *part_b = nullptr;         // block partials
     long long npart = 0;
     double* red = nullptr;                               // 2 doubles on the device (+ dflag)
     int* dflag = nullptr;                                // bounded-wait error flag, inside red
+    unsigned wait_polls = ples::kSpinLimit;              // polls of a bounded device wait before it gives up
     double* h_red = nullptr;                             // pinned host copy
     double* norm_scratch = nullptr;  // device address of the library's fixed residual scratch (this device)
     double *fi_c = nullptr, *rhs_c = nullptr;            // compact staging

@@ -68,14 +68,16 @@ __host__ __device__ constexpr unsigned line_tma_chunk_bytes(bool zin, bool zk) {
 // Zebra half-sweep over the planes k = 2*blockIdx.x + 1 + kpar, 32 lines per
 // CTA (blockIdx.y).  pin is the old field (map pA if pin_is_a, else pB), pk
 // holds the planes k-1 and k+1 (map by pk_is_a); zk: those planes are zero.
-// A transfer that does not complete within the bounded wait sets *err and
-// the CTA leaves without writing.
+// A transfer that does not complete within the bounded wait (wait_polls
+// polls of its mbarrier, and 2 s) sets *err and the CTA leaves without
+// writing, after a second bounded wait (the default limits) for the copies
+// it still has in flight.
 template <bool ZIN>
 __global__ void __launch_bounds__(256) k_line_relax_tma(const __grid_constant__ LineMaps maps, Geom g,
                                                         Coef<float> c, const float* __restrict__ cpa,
                                                         const float* __restrict__ pin, float* pout, float omega,
                                                         int kpar, int zk, int pin_is_a, int pk_is_a,
-                                                        int* __restrict__ err) {
+                                                        int* __restrict__ err, unsigned wait_polls) {
     extern __shared__ __align__(128) unsigned char smem_tma[];
     float* buf = reinterpret_cast<float*>(smem_tma);
     const int nj = g.ny + 2, ny = g.ny;
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(256) k_line_relax_tma(const __grid_constant__ 
     int failed = -1;
     for (int ch = 0; ch < nchunk; ++ch) {
         const float* b = buf + (ch % kNB) * ChunkLayout::SIZE;
-        const bool ok = mbar_wait(bar + (ch % kNB), (unsigned)((ch / kNB) & 1));
+        const bool ok = mbar_wait(bar + (ch % kNB), (unsigned)((ch / kNB) & 1), wait_polls);
         if (__syncthreads_or(!ok)) { failed = ch; break; }
         const int jj = w;  // row of this warp inside the chunk
         const int j = ch * kRC + jj;

@@ -345,16 +345,21 @@ __device__ __forceinline__ void seg_thomas(T* G, const T* AL, const T* CP, int n
 // forward sweep of tridag.f03): c'(0) = -1, c'(j) = A2(j) / (b(j) - A2(j-1)
 // c'(j-1)).  The operator depends on the coefficients only, so c' is built
 // once per level; the smoothers then need one division per row in their
-// parallel phase and a pure FMA chain in the sequential one.
+// parallel phase and a pure FMA chain in the sequential one.  With im given,
+// the pivot reciprocal 1/m(j) of every row j = 0..ny+1 is stored as well
+// (the expressions the line smoothers evaluate, 1 on identity rows), so
+// the pair-build smoother needs no division at all.
 template <typename T>
-__global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp) {
+__global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp, T* __restrict__ im) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int k = blockIdx.y + 1;
     if (i > g.nx) return;
     // a row whose coefficients are all zero (a solid cell of an immersed-
     // boundary mask, or the wall row next to one) is an identity row: c' = 0
-    T prev = ld(c.a2, g.at(i, 0, k)) == T(0) ? T(0) : T(-1);
+    const T a20 = ld(c.a2, g.at(i, 0, k));
+    T prev = a20 == T(0) ? T(0) : T(-1);
     cp[g.at(i, 0, k)] = prev;
+    if (im) im[g.at(i, 0, k)] = a20 == T(0) ? T(1) : T(1) / a20;
     for (int j = 1; j <= g.ny; ++j) {
         const long long q = g.at(i, j, k);
         const T a = ld(c.a2, q - g.sj), cc = ld(c.a2, q);
@@ -362,10 +367,16 @@ __global__ void k_line_lu(Geom g, Coef<T> c, T* __restrict__ cp) {
         const T ae = !g.px && i == g.nx ? T(0) : ld(c.a1, q), aw = !g.px && i == 1 ? T(0) : ld(c.a1, q - 1);
         const T af = !g.pz && k == g.nz ? T(0) : ld(c.a3, q), ab = !g.pz && k == 1 ? T(0) : ld(c.a3, q - g.sk);
         const T b = -(cc + a + ae + aw + af + ab);
+        if (im) im[q] = b == T(0) ? T(1) : T(1) / (b - a * prev);
         prev = b == T(0) ? T(0) : cc / (b - a * prev);
         cp[q] = prev;
     }
     cp[g.at(i, g.ny + 1, k)] = T(0);
+    if (im) {  // the top wall row: a2(ny) x(ny+1) - a2(ny) x(ny) = f
+        const T as = ld(c.a2, g.at(i, g.ny, k));
+        const T a = -as;
+        im[g.at(i, g.ny + 1, k)] = as == T(0) ? T(1) : T(1) / (as - a * prev);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -967,6 +978,53 @@ __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c,
                                                           float* __restrict__ pout, const float* __restrict__ rh,
                                                           float omega, int kpar, int zk) {
     k_line_relax_x2_blk<ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
+}
+
+// ---------------------------------------------------------------------------
+// Multicolour point SOR: the device form of solut_sndrcv_sor
+// (multigrid.f03:656-1010, selected by islor = 0).  The reference sweeps the
+// cells lexicographically and refreshes the ghost rows before every sweep;
+// here the cells of one colour -- (i & 1) + 2 (j & 1) + 4 (k & 1) -- are
+// updated at once: each of the 18 neighbours of the 19-point stencil differs
+// from its cell in the parity of i, j or k, so no two cells of a colour are
+// coupled (periodic directions need an even cell count, checked when the
+// handle is created).  An interior cell takes pr += omega resi / den with
+// resi = L(pr) - rh and den the sum of its six normal coefficients
+// (multigrid.f03:840-913, scaled coefficients); a ghost cell of the wall rows
+// j = 0 and ny+1 takes its homogeneous relation (mul_boun_sndrcv,
+// multigrid.f03:1166-1186) solved for itself, or with FS at the top the
+// free-surface relation of :1188-1222 with PrS0 = 0 (the correction's), so
+// the ghost rows join the sweep where the reference runs five passes of its
+// fill before it.  In place, one launch per colour; identity rows of a mask
+// (no coefficients) keep their value.
+template <typename T, bool FS>
+__global__ void k_point_sor(Geom g, Coef<T> c, T* __restrict__ p, const T* __restrict__ rh, T omega, int colour) {
+    const int ci = colour & 1, cj = (colour >> 1) & 1, ck = (colour >> 2) & 1;
+    const int i = 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x) + (ci ? 1 : 2);
+    const int j = 2 * (int)(blockIdx.y * blockDim.y + threadIdx.y) + cj;
+    const int k = 2 * (int)blockIdx.z + (ck ? 1 : 2);
+    if (i > g.nx || j > g.ny + 1 || k > g.nz) return;
+    const long long q = g.at(i, j, k), sj = g.sj, sk = g.sk;
+    T v;
+    if (j == 0) {  // bottom wall: flux through face 0 is zero
+        const T a2 = c.a2[q];
+        if (a2 == T(0)) return;
+        const long long q1 = q + sj;
+        v = p[q1] + (c.b21[q] * (p[q1 + 1] + p[q + 1] - p[q1 - 1] - p[q - 1]) +
+                     c.b23[q] * (p[q1 + sk] + p[q + sk] - p[q1 - sk] - p[q - sk])) / a2;
+    } else if (j == g.ny + 1) {  // top: wall (flux through face ny zero) or free surface
+        const long long qn = q - sj;
+        const T a2 = c.a2[qn];
+        if (a2 == T(0)) return;
+        const T cross = (c.b21[qn] * (p[q + 1] + p[qn + 1] - p[q - 1] - p[qn - 1]) +
+                         c.b23[qn] * (p[q + sk] + p[qn + sk] - p[q - sk] - p[qn - sk])) / a2;
+        v = FS ? cross - p[qn] : p[qn] - cross;
+    } else {
+        const T den = c.a1[q] + c.a1[q - 1] + c.a2[q] + c.a2[q - sj] + c.a3[q] + c.a3[q - sk];
+        if (den == T(0)) return;
+        v = p[q] + omega * cell_residual(g, c, p, rh, q) / den;
+    }
+    store_periodic(g, p, i, j, k, v);
 }
 
 // ---------------------------------------------------------------------------

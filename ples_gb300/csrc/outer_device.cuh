@@ -251,10 +251,14 @@ __device__ __forceinline__ void k_update_blk(Geom g, double* __restrict__ x, con
     }
 }
 // FP64 wall ghost rows j = 0 and ny+1 from the current field
-// (mul_boun_sndrcv, multigrid.f03:1160-1186, freesurface = 0), written to a
-// side buffer so that one pass is a Jacobi step (race-free, deterministic).
+// (mul_boun_sndrcv, multigrid.f03:1160-1186), written to a side buffer so
+// that one pass is a Jacobi step (race-free, deterministic).  fs: the top
+// row takes the free-surface relation of multigrid.f03:1188-1222 instead,
+// pr(ny+1) = 2 PrS0 - (pr(ny) - cross terms / r22), PrS0 = prs(i,k)
+// ((1:nx,1:nz), or zero when null).
 __device__ __forceinline__ void k_wall_compute_blk(Geom g, Coef<double> c, const double* __restrict__ p, double* __restrict__ w,
-                               const double* __restrict__ cs3, const double* __restrict__ cs4, double an_dt, const Blk& B) {
+                               const double* __restrict__ cs3, const double* __restrict__ cs4, double an_dt, const Blk& B,
+                               int fs = 0, const double* __restrict__ prs = nullptr) {
     const int i = B.x * blockDim.x + threadIdx.x + 1;
     const int k = B.y * blockDim.y + threadIdx.y + 1;
     const int side = B.z;
@@ -280,10 +284,16 @@ __device__ __forceinline__ void k_wall_compute_blk(Geom g, Coef<double> c, const
             w[widx] = 0.0;
             return;
         }
+        const double cross = (c.b21[qn] * (p[qt + 1] + p[qn + 1] - p[qt - 1] - p[qn - 1]) +
+                              c.b23[qn] * (p[qt + sk] + p[qn + sk] - p[qt - sk] - p[qn - sk])) / a2;
+        if (fs) {
+            const double s0 = prs ? prs[(long long)(k - 1) * g.nx + (i - 1)] : 0.0;
+            w[widx] = s0 * 2.0 - (p[qn] - cross);
+            return;
+        }
         double v = p[qn];
         if (cs4) v += an_dt * cs4[(long long)(k - 1) * g.nx + (i - 1)] / a2;
-        v -= (c.b21[qn] * (p[qt + 1] + p[qn + 1] - p[qt - 1] - p[qn - 1]) +
-              c.b23[qn] * (p[qt + sk] + p[qn + sk] - p[qt - sk] - p[qn - sk])) / a2;
+        v -= cross;
         w[widx] = v;
     }
 }

@@ -19,6 +19,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstddef>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -128,8 +129,9 @@ __global__ void k_update(Geom g, double* __restrict__ x, const Te* __restrict__ 
 }
 
 __global__ void k_wall_compute(Geom g, Coef<double> c, const double* __restrict__ p, double* __restrict__ w,
-                               const double* __restrict__ cs3, const double* __restrict__ cs4, double an_dt) {
-    k_wall_compute_blk(g, c, p, w, cs3, cs4, an_dt, hw_blk());
+                               const double* __restrict__ cs3, const double* __restrict__ cs4, double an_dt,
+                               int fs, const double* __restrict__ prs) {
+    k_wall_compute_blk(g, c, p, w, cs3, cs4, an_dt, hw_blk(), fs, prs);
 }
 
 __global__ void k_wall_scatter(Geom g, double* __restrict__ p, const double* __restrict__ w) {
@@ -344,6 +346,8 @@ int set_x2_smem_attr(ples_mg_handle* h, size_t smem) {
     current = smem;
     CK(cudaFuncSetAttribute(k_line_relax_x2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_x2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_p2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_p2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
 }
 
@@ -461,12 +465,40 @@ void side_fill(ples_mg_handle* h, const Geom& g, const Coef<T>& c, T* p, T* p2, 
     h->launches += 3;
 }
 
+// nu sweeps of the multicolour point SOR (islor = 0), in place on L.p
+template <typename T>
+void smooth_point(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
+    if (zero) cudaMemsetAsync(L.p, 0, sizeof(T) * (size_t)L.g.n, h->st);
+    const Coef<T> c = coef_of<T>(L);
+    const bool walls = !L.g.px || !L.g.pz;
+    const dim3 blk(32, 4), grd((L.g.nx / 2 + 31) / 32, ((L.g.ny + 3) / 2 + 3) / 4, (L.g.nz + 1) / 2);
+    for (int s = 0; s < nu; ++s) {
+        if (walls) side_fill<T>(h, L.g, c, (T*)L.p, nullptr, nullptr, 0.0, zero && s == 0);
+        timed_begin(h, KIND_LINE, level);
+        for (int colour = 0; colour < 8; ++colour) {
+            if (h->fs)
+                k_point_sor<T, true><<<grd, blk, 0, h->st>>>(L.g, c, (T*)L.p, (const T*)L.rh, T(h->omega), colour);
+            else
+                k_point_sor<T, false><<<grd, blk, 0, h->st>>>(L.g, c, (T*)L.p, (const T*)L.rh, T(h->omega), colour);
+        }
+        h->launches += 8;
+        timed_end(h, KIND_LINE, level);
+    }
+    if (walls && nu > 0)
+        for (int r = 0; r < 2; ++r) side_fill<T>(h, L.g, c, (T*)L.p, nullptr, nullptr, 0.0, false);
+}
+
 template <typename T>
 void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
+    if (h->smoother == 3) {
+        smooth_point<T>(h, L, nu, level, zero);
+        return;
+    }
     if (zero && nu == 0) cudaMemsetAsync(L.p, 0, sizeof(T) * (size_t)L.g.n, h->st);
     const Coef<T> c = coef_of<T>(L);
     const T om = T(h->omega);
     const bool x2 = std::is_same<T, float>::value && h->smoother == 0 && L.line_threads == 1024 && L.x2_ok;
+    const bool p2 = std::is_same<T, float>::value && h->smoother == 0 && L.line_threads == 2048 && L.x2_ok;
     const int nt = h->smoother == 1 ? std::min(L.line_threads, 256) : std::min(L.line_threads, 512);
     const size_t smem = line_smem<T>(L.g, nt);
     const T* cp = (const T*)L.cp;
@@ -487,15 +519,27 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
                 const int a_in = pin == L.pA, a_out = pout == L.pA;
                 if (zin) {
                     k_line_relax_tma<true><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 0, 1, a_in,
-                                                                     a_in, h->dflag);
+                                                                     a_in, h->dflag, h->wait_polls);
                     k_line_relax_tma<true><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 1, 0, a_in,
-                                                                     a_out, h->dflag);
+                                                                     a_out, h->dflag, h->wait_polls);
                 } else {
                     k_line_relax_tma<false><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 0, 0, a_in,
-                                                                      a_in, h->dflag);
+                                                                      a_in, h->dflag, h->wait_polls);
                     k_line_relax_tma<false><<<grd, 256, sm, h->st>>>(L.maps, L.g, c, cp, pin, pout, om, 1, 0, a_in,
-                                                                      a_out, h->dflag);
+                                                                      a_out, h->dflag, h->wait_polls);
                 }
+                h->launches += 2;
+                staged = true;
+            }
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            if (p2) {  // zebra on 64-line tiles, rows built two lines per lane
+                dim3 grd((L.g.nx + 63) / 64, (L.g.nz + 1) / 2);
+                const size_t sm = line_smem_x2(L.g);
+                auto kern = zin ? k_line_relax_p2<true> : k_line_relax_p2<false>;
+                const float* im = (const float*)L.im;
+                kern<<<grd, 256, sm, h->st>>>(L.g, c, cp, im, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
+                kern<<<grd, 256, sm, h->st>>>(L.g, c, cp, im, pin, pout, pout, (const T*)L.rh, om, 1, 0);
                 h->launches += 2;
                 staged = true;
             }
@@ -625,7 +669,8 @@ void wall_fill(ples_mg_handle* h, double* p, const double* const cs[6], double a
     for (int s = 0; s < passes; ++s) {
         timed_begin(h, KIND_WALL, 1);
         k_wall_compute<<<dim3((g.nx + 31) / 32, (g.nz + 3) / 4, 2), blk, 0, h->st>>>(
-            g, c, p, h->wbuf, cs ? cs[2] : nullptr, cs ? cs[3] : nullptr, an_dt);
+            g, c, p, h->wbuf, cs ? cs[2] : nullptr, cs ? cs[3] : nullptr, an_dt, h->fs ? 1 : 0,
+            an_dt != 0.0 ? h->prs : nullptr);
         k_wall_scatter<<<dim3((g.nx + 2 + 31) / 32, (g.nz + 2 + 3) / 4, 2), blk, 0, h->st>>>(g, p, h->wbuf);
         h->launches += 2;
         side_fill<double>(h, g, c, p, nullptr, cs, an_dt, false);
@@ -693,7 +738,8 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         }
         if (any) flux = ((sum[1] - sum[0]) + (sum[3] - sum[2]) + (sum[5] - sum[4])) / dt;
     }
-    const double shift = (sb - flux) / N;
+    // a free surface fixes the pressure level: no null space, no compatibility condition
+    const double shift = h->fs ? 0.0 : (sb - flux) / N;
     {
         dim3 blk(32, 4), grd((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
         k_add_interior<<<grd, blk, 0, h->st>>>(g, h->b, -shift, h->mask[0]);
@@ -743,7 +789,8 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     if (graphs) {
         std::vector<long long> key = {(long long)sizeof(T), h->inner_cycles, h->nu_pre, h->nu_post, h->nu_coarse,
                                       h->timed_kind, h->timed_level,
-                                      h->smoother, h->wall_passes, (long long)(uintptr_t)h->cs_c[0],
+                                      h->smoother, h->wall_passes, (long long)h->wait_polls,
+                                      (long long)(uintptr_t)h->cs_c[0],
                                       (long long)(uintptr_t)h->cs_c[1], (long long)(uintptr_t)h->cs_c[2],
                                       (long long)(uintptr_t)h->cs_c[3], (long long)(uintptr_t)h->cs_c[4],
                                       (long long)(uintptr_t)h->cs_c[5]};
@@ -826,11 +873,13 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         k_zero_solid<double><<<grid1(g.n), 256, 0, h->st>>>(g, h->x, h->mask[0]);
         ++h->launches;
     }
-    double sx = 0.0;
-    rc = sum_interior(h, h->x, 0, &sx);
-    if (rc) return rc;
-    k_add_box<<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, -sx / N, h->mask[0]);
-    ++h->launches;
+    if (!h->fs) {
+        double sx = 0.0;
+        rc = sum_interior(h, h->x, 0, &sx);
+        if (rc) return rc;
+        k_add_box<<<box_grid(g), dim3(32, 4), 0, h->st>>>(g, h->x, -sx / N, h->mask[0]);
+        ++h->launches;
+    }
     CK(cudaGetLastError());
     st->outer_iterations = it;
     st->vcycles = vcyc;
@@ -858,7 +907,13 @@ int validate(const ples_mg_desc* d, ples_mg_handle* h) {
     if (!(d->dt > 0.0) || !std::isfinite(d->dt)) return fail(h, PLES_MG_BAD_ARG, "dt must be positive");
     if (d->nlevmax < 0 || d->nu_pre < 0 || d->nu_post < 0 || d->nu_coarse < 0 || d->inner_cycles < 0)
         return fail(h, PLES_MG_BAD_ARG, "negative level or sweep count");
-    if (d->smoother < 0 || d->smoother > 2) return fail(h, PLES_MG_BAD_ARG, "unknown smoother %d", d->smoother);
+    if (d->smoother < 0 || d->smoother > 3) return fail(h, PLES_MG_BAD_ARG, "unknown smoother %d", d->smoother);
+    if (d->freesurface != 0 && d->freesurface != 1)
+        return fail(h, PLES_MG_BAD_ARG, "freesurface must be 0 or 1");
+    if (d->freesurface && d->smoother != 3)
+        return fail(h, PLES_MG_BAD_ARG,
+                    "the free surface needs the point smoother (smoother 3, islor = 0): the reference's line SOR "
+                    "keeps the wall relation (multigrid.f03:2019)");
     if (d->coarsening != 0 && d->coarsening != 1)
         return fail(h, PLES_MG_BAD_ARG, "unknown coarsening %d", d->coarsening);
     if (d->jx % 2 || d->jz % 2) return fail(h, PLES_MG_BAD_ARG, "jx and jz must be even");
@@ -1032,6 +1087,11 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
                     add(1, 1, 0, -B21(q)); add(1, 0, 0, -B21(q)); add(-1, 1, 0, B21(q)); add(-1, 0, 0, B21(q));
                     add(0, 1, 1, -B23(q)); add(0, 0, 1, -B23(q)); add(0, 1, -1, B23(q)); add(0, 0, -1, B23(q));
                     R[n] = -1.0;
+                } else if (j == nj - 1 && h->fs) {  // top free-surface relation (PrS0 = 0), face ny
+                    const long long q = g.at(i, ny, k);
+                    add(0, 0, 0, A2(q)); add(0, -1, 0, A2(q));
+                    add(1, 0, 0, -B21(q)); add(1, -1, 0, -B21(q)); add(-1, 0, 0, B21(q)); add(-1, -1, 0, B21(q));
+                    add(0, 0, 1, -B23(q)); add(0, -1, 1, -B23(q)); add(0, 0, -1, B23(q)); add(0, -1, -1, B23(q));
                 } else if (j == nj - 1) {  // top wall relation, face ny
                     const long long q = g.at(i, ny, k);
                     add(0, 0, 0, A2(q)); add(0, -1, 0, -A2(q));
@@ -1080,6 +1140,13 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         } else {
             K[(size_t)n * m + u] = 1.0;
         }
+    }
+    if (h->fs) {  // a free surface removes the null space: the border unknown decouples
+        for (int u = 0; u < n; ++u) {
+            K[(size_t)u * m + n] = 0.0;
+            K[(size_t)n * m + u] = 0.0;
+        }
+        K[(size_t)n * m + n] = 1.0;
     }
     // Gauss-Jordan inverse with partial pivoting, on the device
     std::vector<int> perm0(m);
@@ -1211,7 +1278,8 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     CK(cudaSetDevice(h->dev));
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     h->smoother = d->smoother;
-    h->omega = d->omega > 0.0 ? d->omega : (d->smoother != 1 ? 1.3 : 0.8);
+    h->omega = d->omega > 0.0 ? d->omega : (d->smoother == 1 ? 0.8 : (d->smoother == 3 ? 1.0 : 1.3));
+    h->fs = d->freesurface != 0;
     h->nu_pre = d->nu_pre ? d->nu_pre : 2;
     h->nu_post = d->nu_post ? d->nu_post : 2;
     // sweeps on a smoothed coarsest level (x / z walls, no dense inverse): 10,
@@ -1328,11 +1396,15 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         if ((rc = dalloc(h, &L.p, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.p2, es * (size_t)L.g.n)) ||
             (rc = dalloc(h, &L.rh, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.cp, es * (size_t)L.g.n)))
             return rc;
+        // the 64-line-tile forms: FP32 zebra with periodic x and z, nx even
+        L.x2_ok = mixed && h->smoother == 0 && L.g.px && L.g.pz && L.g.nx % 2 == 0 && L.g.nz >= 2 &&
+                  line_smem_x2(L.g) <= 227 * 1024;
+        if (L.x2_ok && (rc = dalloc(h, &L.im, sizeof(float) * (size_t)L.g.n))) return rc;
         dim3 lg((L.g.nx + 127) / 128, L.g.nz);
         if (mixed)
-            k_line_lu<float><<<lg, 128, 0, h->st>>>(L.g, L.cf, (float*)L.cp);
+            k_line_lu<float><<<lg, 128, 0, h->st>>>(L.g, L.cf, (float*)L.cp, (float*)L.im);
         else
-            k_line_lu<double><<<lg, 128, 0, h->st>>>(L.g, L.cd, (double*)L.cp);
+            k_line_lu<double><<<lg, 128, 0, h->st>>>(L.g, L.cd, (double*)L.cp, nullptr);
         CK(cudaGetLastError());
         size_t sm = mixed ? line_smem<float>(L.g) : line_smem<double>(L.g);
         if (sm > 227 * 1024) return fail(h, PLES_MG_BAD_ARG, "eta lines too long for shared memory");
@@ -1343,9 +1415,6 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
             const size_t sw = mixed ? line_smem<float>(L.g, 512) : line_smem<double>(L.g, 512);
             L.line_threads = ctas < 2 * 152 && sw <= 227 * 1024 ? 512 : 256;
         }
-        // the 64-line-tile form: FP32 zebra with periodic x and z, nx even
-        L.x2_ok = mixed && h->smoother == 0 && L.g.px && L.g.pz && L.g.nx % 2 == 0 && L.g.nz >= 2 &&
-                  line_smem_x2(L.g) <= 227 * 1024;
         if (L.x2_ok) {
             if ((rc = set_x2_smem_attr(h, line_smem_x2(L.g)))) return rc;
             // by default where its launch has at least 96 CTAs: measured
@@ -1372,6 +1441,20 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     }
     if (smem_max > 227 * 1024) return fail(h, PLES_MG_BAD_ARG, "eta lines too long for shared memory");
     if ((rc = mixed ? set_smem_attrs<float>(h, smem_max) : set_smem_attrs<double>(h, smem_max))) return rc;
+    if (h->smoother == 3) {  // the colours decouple a periodic direction only with an even cell count
+        const int nsm = h->coarse_S ? nl - 1 : nl;
+        for (int n = 0; n < nsm; ++n) {
+            const Geom& gn = h->L[n].g;
+            if ((gn.px && gn.nx % 2) || (gn.pz && gn.nz % 2))
+                return fail(h, PLES_MG_BAD_ARG,
+                            "the point smoother needs even cell counts in periodic directions: level %d is %dx%dx%d "
+                            "(set nlevmax)", n + 1, gn.nx, gn.ny, gn.nz);
+        }
+    }
+    if (h->fs) {  // the surface pressure of the free surface (PrS0), zero until set
+        if ((rc = dalloc(h, (void**)&h->prs, 8 * (size_t)jx * jz))) return rc;
+        CK(cudaMemsetAsync(h->prs, 0, 8 * (size_t)jx * jz, h->st));
+    }
     const Geom& g = h->L[0].g;
     if ((rc = dalloc(h, (void**)&h->x, 8 * (size_t)g.n)) || (rc = dalloc(h, (void**)&h->b, 8 * (size_t)g.n)) ||
         (rc = dalloc(h, (void**)&h->wbuf, 8 * 2 * (size_t)g.nx * g.nz)) ||
@@ -2101,17 +2184,70 @@ int ples_mg_set_line_threads(ples_mg_handle* h, int level, int threads) {
     LevelData& L = h->L[level - 1];
     const bool mixed = h->d.precision == PLES_MG_PREC_MIXED;
     size_t need = 0;
-    if (threads == 1024) {
+    if (threads == 1024 || threads == 2048) {
         if (!L.x2_ok) return fail(h, PLES_MG_BAD_ARG, "the 64-line-tile smoother does not apply at level %d", level);
         need = line_smem_x2(L.g);
     } else if (threads == 128 || threads == 256 || threads == 512) {
         need = mixed ? line_smem<float>(L.g, threads) : line_smem<double>(L.g, threads);
     } else {
-        return fail(h, PLES_MG_BAD_ARG, "smoother form %d is not 128, 256, 512 or 1024", threads);
+        return fail(h, PLES_MG_BAD_ARG, "smoother form %d is not 128, 256, 512, 1024 or 2048", threads);
     }
     if (need > 227 * 1024) return fail(h, PLES_MG_BAD_ARG, "smoother form %d needs %zu B of shared memory", threads, need);
     L.line_threads = threads;
     return PLES_MG_OK;
+}
+
+int ples_mg_set_wait_limit(ples_mg_handle* h, long long polls) {
+    if (!h) return PLES_MG_BAD_ARG;
+    if (polls > (long long)kSpinLimit) return fail(h, PLES_MG_BAD_ARG, "wait limit above %u polls", kSpinLimit);
+    h->wait_polls = polls < 0 ? kSpinLimit : (unsigned)polls;
+    return PLES_MG_OK;
+}
+
+int ples_mg_abi_layout(int* abi_version, long long* desc_size, long long* stats_size, long long* desc_offsets,
+                       long long* stats_offsets) {
+    if (abi_version) *abi_version = PLES_MG_ABI_VERSION;
+    if (desc_size) *desc_size = (long long)sizeof(ples_mg_desc);
+    if (stats_size) *stats_size = (long long)sizeof(ples_mg_stats);
+    if (desc_offsets) {
+        const long long o[PLES_MG_DESC_FIELDS] = {
+            (long long)offsetof(ples_mg_desc, jx), (long long)offsetof(ples_mg_desc, jy),
+            (long long)offsetof(ples_mg_desc, jz), (long long)offsetof(ples_mg_desc, ip),
+            (long long)offsetof(ples_mg_desc, jp), (long long)offsetof(ples_mg_desc, kp),
+            (long long)offsetof(ples_mg_desc, nlevmax), (long long)offsetof(ples_mg_desc, omega),
+            (long long)offsetof(ples_mg_desc, precision), (long long)offsetof(ples_mg_desc, coords_layout),
+            (long long)offsetof(ples_mg_desc, x), (long long)offsetof(ples_mg_desc, y),
+            (long long)offsetof(ples_mg_desc, z), (long long)offsetof(ples_mg_desc, dt),
+            (long long)offsetof(ples_mg_desc, device), (long long)offsetof(ples_mg_desc, nu_pre),
+            (long long)offsetof(ples_mg_desc, nu_post), (long long)offsetof(ples_mg_desc, nu_coarse),
+            (long long)offsetof(ples_mg_desc, inner_cycles), (long long)offsetof(ples_mg_desc, smoother),
+            (long long)offsetof(ples_mg_desc, coarsening), (long long)offsetof(ples_mg_desc, solid),
+            (long long)offsetof(ples_mg_desc, tipo), (long long)offsetof(ples_mg_desc, freesurface)};
+        for (int f = 0; f < PLES_MG_DESC_FIELDS; ++f) desc_offsets[f] = o[f];
+    }
+    if (stats_offsets) {
+        const long long o[PLES_MG_STATS_FIELDS] = {
+            (long long)offsetof(ples_mg_stats, outer_iterations), (long long)offsetof(ples_mg_stats, vcycles),
+            (long long)offsetof(ples_mg_stats, rel_residual), (long long)offsetof(ples_mg_stats, max_residual),
+            (long long)offsetof(ples_mg_stats, rhs_norm), (long long)offsetof(ples_mg_stats, rhs_mean_removed),
+            (long long)offsetof(ples_mg_stats, seconds), (long long)offsetof(ples_mg_stats, status)};
+        for (int f = 0; f < PLES_MG_STATS_FIELDS; ++f) stats_offsets[f] = o[f];
+    }
+    return PLES_MG_OK;
+}
+
+int ples_mg_set_surface_pressure(ples_mg_handle* h, const double* next_prs) {
+    if (!h) return PLES_MG_BAD_ARG;
+    if (!h->fs) return fail(h, PLES_MG_BAD_ARG, "the handle has no free surface (desc.freesurface)");
+    return with_device(h, [&]() -> int {
+        const size_t bytes = 8 * (size_t)h->d.jx * h->d.jz;
+        if (next_prs)
+            CK(cudaMemcpyAsync(h->prs, next_prs, bytes, cudaMemcpyHostToDevice, h->st));
+        else
+            CK(cudaMemsetAsync(h->prs, 0, bytes, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        return PLES_MG_OK;
+    });
 }
 
 int ples_mg_get_line_threads(const ples_mg_handle* h, int level, int* threads) {
@@ -2181,14 +2317,15 @@ int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) 
         int rc, tried = 0;
         double ms = 0.0;
         ples_mg_stats st;
-        const int nsmooth = h->coarse_S ? h->nlev - 1 : h->nlev;
+        // the line smoother's form per level (the point smoother has one form)
+        const int nsmooth = h->smoother == 3 ? 0 : (h->coarse_S ? h->nlev - 1 : h->nlev);
         for (int n = 0; n < nsmooth; ++n) {
             double best = 1e300;
             int bt = h->L[n].line_threads;
-            for (int t : {128, 256, 512, 1024}) {
+            for (int t : {128, 256, 512, 1024, 2048}) {
                 const LevelData& Ln = h->L[n];
-                if (t == 1024 && !Ln.x2_ok) continue;
-                const size_t need = t == 1024 ? line_smem_x2(Ln.g)
+                if (t >= 1024 && !Ln.x2_ok) continue;
+                const size_t need = t >= 1024 ? line_smem_x2(Ln.g)
                                     : h->d.precision == PLES_MG_PREC_MIXED ? line_smem<float>(Ln.g, t)
                                                                           : line_smem<double>(Ln.g, t);
                 if (need > 227 * 1024) continue;

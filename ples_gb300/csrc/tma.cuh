@@ -48,11 +48,12 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned by
                  : "memory");
 }
 
-// bounded wait for the phase with the given parity; false on time-out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// bounded wait for the phase with the given parity: at most `limit` polls
+// and kWaitNs of wall time; false on time-out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit = kSpinLimit) {
     const unsigned a = smem_u32(bar);
     unsigned long long t0 = 0;
-    for (unsigned it = 0; it < kSpinLimit; ++it) {
+    for (unsigned it = 0; it < limit; ++it) {
         if ((it & 255u) == 255u) {
             const unsigned long long t = global_ns();
             if (t0 == 0) t0 = t;

@@ -41,7 +41,7 @@ class Desc(C.Structure):
                 ("z", C.POINTER(C.c_double)), ("dt", C.c_double), ("device", C.c_int),
                 ("nu_pre", C.c_int), ("nu_post", C.c_int), ("nu_coarse", C.c_int),
                 ("inner_cycles", C.c_int), ("smoother", C.c_int), ("coarsening", C.c_int),
-                ("solid", C.c_void_p), ("tipo", C.c_void_p)]
+                ("solid", C.c_void_p), ("tipo", C.c_void_p), ("freesurface", C.c_int)]
 
 
 class Tuning(C.Structure):
@@ -71,7 +71,8 @@ EXPORTS = ("ples_mg_create", "ples_mg_solve", "ples_mg_solve_device", "ples_mg_d
            "ples_mg_batch_last_error", "ples_mg_batch_destroy", "ples_srv_create", "ples_srv_submit",
            "ples_srv_wait", "ples_srv_report", "ples_srv_destroy", "ples_mg_autotune", "ples_mg_project",
            "ples_mg_step", "ples_mg_residual_norms_device", "ples_mg_read_grid", "ples_mg_potenziale_ibm",
-           "ples_mg_set_line_threads", "ples_mg_get_line_threads")
+           "ples_mg_set_line_threads", "ples_mg_get_line_threads", "ples_mg_set_surface_pressure",
+           "ples_mg_abi_layout", "ples_mg_set_wait_limit")
 KERNEL_KINDS = {"line": 0, "restrict": 1, "prolong": 2, "outer": 3}
 
 
@@ -109,6 +110,10 @@ def load(build=True):
     L.ples_mg_autotune.argtypes = [vp, vp, C.POINTER(Tuning)]
     L.ples_mg_set_line_threads.argtypes = [vp, C.c_int, C.c_int]
     L.ples_mg_get_line_threads.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    L.ples_mg_set_surface_pressure.argtypes = [vp, vp]
+    L.ples_mg_set_wait_limit.argtypes = [vp, C.c_longlong]
+    LL = C.POINTER(C.c_longlong)
+    L.ples_mg_abi_layout.argtypes = [C.POINTER(C.c_int), LL, LL, LL, LL]
     L.ples_mg_project.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_step.argtypes = [vp] + [vp] * 7 + [C.c_double, C.c_int, C.POINTER(Stats)]
     L.ples_mg_read_grid.argtypes = [C.c_char_p, vp, vp, vp, vp, vp]
@@ -166,7 +171,8 @@ class Multigrid:
 
     def __init__(self, x, y, z, ip=0, jp=1, kp=0, precision="mixed", dt=1.0, device=0,
                  nlevmax=0, omega=0.0, nu_pre=0, nu_post=0, nu_coarse=0, inner_cycles=0,
-                 smoother=0, coarsening=0, coords_layout=COORDS_NODES, solid=None, tipo=None):
+                 smoother=0, coarsening=0, coords_layout=COORDS_NODES, solid=None, tipo=None,
+                 freesurface=0):
         self._L = load()
         self._x, self._y, self._z = _f64(x), _f64(y), _f64(z)
         if coords_layout == COORDS_NODES:
@@ -185,6 +191,7 @@ class Multigrid:
         d.dt, d.device = dt, device
         d.nu_pre, d.nu_post, d.nu_coarse = nu_pre, nu_post, nu_coarse
         d.inner_cycles, d.smoother, d.coarsening = inner_cycles, smoother, coarsening
+        d.freesurface = freesurface
         self._solid = None
         if solid is not None:  # immersed-boundary mask (jx, jy, jz), nonzero = solid
             self._solid = np.asfortranarray(np.asarray(solid) != 0, dtype=np.uint8)
@@ -347,6 +354,21 @@ class Multigrid:
         """Smoother form at one level (1-based): 128, 256 or 512 threads on
         32-line tiles, or 1024 for the 64-line tiles (ples_mg_set_line_threads)."""
         self._check(self._L.ples_mg_set_line_threads(self._h, level, threads))
+
+    def set_surface_pressure(self, next_prs=None):
+        """Surface pressure PrS0 (jx, jz) of a free-surface handle for the
+        following solves (ples_mg_set_surface_pressure); None = zero."""
+        ptr = None
+        if next_prs is not None:
+            self._prs = _f64(next_prs)
+            if self._prs.shape != (self.jx, self.jz):
+                raise ValueError(f"next_prs must be {(self.jx, self.jz)}")
+            ptr = self._prs.ctypes.data
+        self._check(self._L.ples_mg_set_surface_pressure(self._h, ptr))
+
+    def set_wait_limit(self, polls=-1):
+        """Polls of a bounded device wait before it gives up (-1: default)."""
+        self._check(self._L.ples_mg_set_wait_limit(self._h, polls))
 
     def line_threads(self, level):
         """The smoother form at one level (ples_mg_get_line_threads)."""

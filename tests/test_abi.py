@@ -55,11 +55,15 @@ def _desc(**kw):
     return d, keep
 
 
-@pytest.mark.parametrize("field,value", [("jp", 0), ("ip", 2), ("kp", -1), ("jx", 4), ("precision", 7),
-                                         ("coords_layout", 5), ("dt", 0.0), ("smoother", 3), ("jz", 15)])
-def test_bad_descriptor_rejected_without_device(field, value):
+@pytest.mark.parametrize("fields", [{"jp": 0}, {"ip": 2}, {"kp": -1}, {"jx": 4}, {"precision": 7},
+                                    {"coords_layout": 5}, {"dt": 0.0}, {"smoother": 4}, {"jz": 15},
+                                    {"freesurface": 2}, {"freesurface": 1, "smoother": 0}],
+                         ids=lambda f: ",".join(f"{k}={v}" for k, v in f.items()))
+def test_bad_descriptor_rejected_without_device(fields):
+    """Including a free surface without the point smoother: the reference's
+    line SOR keeps the wall relation (multigrid.f03:2019)."""
     lib = mg.load()
-    d, keep = _desc(**{field: value})
+    d, keep = _desc(**fields)
     h = C.c_void_p()
     rc = lib.ples_mg_create(C.byref(d), C.byref(h))
     assert rc == mg.BAD_ARG

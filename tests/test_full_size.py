@@ -4,19 +4,18 @@ C ABI (GPU, slow: each runs the CPU oracle on a grid of the benchmark).
 * channel 256x128x256 (wall amplitude 0.1, stretch 2.5, RHS seed 1): the
   device's zero-mean solution against the oracle's, which the restated
   reference solver (line SOR, 4 levels, emulated MPI ranks) converges to
-  ||r||/||b|| <= 1e-13.  A relative residual bounds the solution error only
-  through the operator's conditioning, which grows with the grid: at this
-  size a field at ||r||/||b|| = 1e-10 can be ~1e-7 away from the exact one
-  (the oracle's own 1e-10 iterate at 128x64x128 is 8e-8 away from its
-  converged solution).  So the device solves to 1e-10 (the benchmark
-  setting) and to 1e-12; the 1e-12 solutions (mixed and FP64) must agree
-  with the oracle within 1e-8 in the L2 and max norms, the 1e-10 one within
-  the distance the oracle's own 1e-10 iterate keeps from the converged
-  solution, times 2.
+  ||r||/||b|| <= 1e-13.  The device solves to 1e-10 (the benchmark
+  setting) and to 1e-12, mixed and FP64; all four agree with the oracle
+  within 1e-8 in the L2 and max norms.  (A relative residual bounds the
+  solution error only through the operator's conditioning: the reference
+  algorithm's own 1e-10 iterate is ~6e-7 away from the converged solution
+  at this size; the device's dense coarsest solve leaves much less of the
+  error in smooth modes.  The test prints both.)
 * the reference's sample deck (gri3dp_in.dat, uniform 32^3) at its own
   settings (Agenerale.in:41-52: point SOR islor = 0, omega 1.6, 4 levels,
-  absolute max-norm stop eps = 1e-8): both solvers stop below eps, and
-  their solutions converged to 1e-13 agree within 1e-8.
+  absolute max-norm stop eps = 1e-8), the device with its point SOR
+  (smoother 3, omega 1.6) and with its line smoother: both solvers stop
+  below eps, and their solutions converged to 1e-13 agree within 1e-8.
 * the 64-grid batch of uneven sizes (seeds 2..65): every member of the
   batched solve within 1e-9 of the same grid solved alone, and one member
   of each of three sizes within 1e-8 of the oracle.
@@ -79,10 +78,7 @@ def test_channel_256x128x256_against_converged_oracle():
                 assert st["status"] == mg.OK and st["rel_residual"] <= tol, (prec, tol, st)
                 l2, mx = _rel(_zm(fi), ref)
                 found[f"{prec}_{tol:g}"] = (l2, mx)
-                if tol == 1e-12:
-                    assert l2 <= SOL_TOL and mx <= SOL_TOL, (prec, found)
-                else:
-                    assert max(l2, mx) <= 2 * max(oracle_gap, SOL_TOL), (prec, found)
+                assert l2 <= SOL_TOL and mx <= SOL_TOL, (prec, tol, found)
     print("channel_256x128x256 solution errors vs the converged oracle:", found)
 
 
@@ -96,7 +92,7 @@ def _deck():
     return d, x, y, z
 
 
-@pytest.mark.parametrize("smoother", [0])
+@pytest.mark.parametrize("smoother", [3, 0], ids=["point_sor", "line_sor"])
 def test_sample_deck_at_its_own_settings(smoother):
     d, x, y, z = _deck()
     s = d["solver"]
@@ -105,7 +101,8 @@ def test_sample_deck_at_its_own_settings(smoother):
     orc = Oracle(x, y, z, islor=s["islor"], omega=s["omega"], nlevmax=s["nlevmultimax"], nproc=2)
     fo, cyc, rmax, _ = orc.multi(rhs, eps=s["eps"], ficycle=s["ficycle"], stop_mode=0)
     assert rmax < s["eps"] and cyc < s["ficycle"]
-    with mg.Multigrid(x, y, z, nlevmax=s["nlevmultimax"], precision="fp64", smoother=smoother) as m:
+    omega = s["omega"] if smoother == 3 else 0.0  # the deck's omega is its point SOR's
+    with mg.Multigrid(x, y, z, nlevmax=s["nlevmultimax"], precision="fp64", smoother=smoother, omega=omega) as m:
         fi, st = m.solve(rhs, rel_tol=0.0, abs_tol=s["eps"], max_cycles=s["ficycle"])
         assert st["status"] == mg.OK and st["max_residual"] < s["eps"], st
         # both stopped by the same absolute test: their fields differ by the
