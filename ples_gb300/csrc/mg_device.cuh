@@ -471,11 +471,16 @@ __device__ __forceinline__ T from_east(T v, T h) {
 // cells beyond it still enter the cross terms of the other faces.
 // RS, slot: as in seg_thomas; ws / nws: the row segment this warp builds and
 // the number of segments (by default the warp's index among the CTA's warps).
-template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false, int RS = 32>
+// FAST: the pivot reciprocals come from ima (1/m per row, k_line_lu) instead
+// of a division per row, and the next rows reach the L2 through one prefetch
+// instruction per row step (lane t fetching the line of array t) instead of
+// one per array.
+template <typename T, bool ZEBRA, bool ZIN, bool WALLS = false, int RS = 32, bool FAST = false>
 __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, const T* __restrict__ cpa,
                                            const T* __restrict__ pin, const T* __restrict__ pk,
                                            const T* __restrict__ rh, T omega, int zk, int i, int k, bool odd, T* G,
-                                           T* AL, T* CP, int ws = -1, int nws = 0, int slot = -1) {
+                                           T* AL, T* CP, int ws = -1, int nws = 0, int slot = -1,
+                                           const T* __restrict__ ima = nullptr) {
     const int lane = threadIdx.x & 31;
     const int w = ws < 0 ? (int)(threadIdx.x >> 5) : ws, nw = ws < 0 ? (int)(blockDim.x >> 5) : nws;
     const int sc = slot < 0 ? lane : slot;
@@ -498,6 +503,20 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
         if (halo) h = ld(a, q + hd);
     };
     const unsigned q0 = at32(g, i, 0, k);
+    // FAST prefetch: lane t < 18 holds array t of the row (the k-1 zeta faces
+    // and the pressure planes offset in advance); one 128-byte line each, the
+    // warp's 32 lines starting on a line boundary
+    const T* pfa = nullptr;
+    if (FAST) {
+        const int t = lane;
+        const T* b = t == 0 ? c.a1 : t == 1 ? c.b12 : t == 2 ? c.b13 : t == 3 ? c.a2 : t == 4 ? c.b21
+                   : t == 5 ? c.b23 : t == 6 || t == 9 ? c.a3 : t == 7 || t == 10 ? c.b31
+                   : t == 8 || t == 11 ? c.b32 : t == 12 ? rh : t == 13 ? cpa : t == 14 ? ima
+                   : t == 15 ? (ZIN ? nullptr : pin) : t == 16 || t == 17 ? (ZIN && zk ? nullptr : pk) : nullptr;
+        const long long off = t >= 9 && t <= 11 ? -(long long)sk
+                            : t == 15 ? (long long)sj : t == 16 ? (long long)sk + sj : t == 17 ? (long long)sj - sk : 0LL;
+        if (b) pfa = b + off - lane;  // the warp's first line: element q0 - lane
+    }
     // window: plane k (P), k+1 (F), k-1 (B); rows j-1 (m), j (0), j+1 (p);
     // h* the halo column of lanes 0 / 31; E*/W* the east / west values of
     // plane k (shuffled once per row and carried)
@@ -534,7 +553,8 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
     for (int j = j0; j < j1; ++j) {
         const unsigned q = q0 + (unsigned)j * sj;
         // every load of the step first: the coefficients of row j ...
-        T a2v = T(0), b21v = T(0), b23v = T(0), cpv = T(0);
+        T a2v = T(0), b21v = T(0), b23v = T(0), cpv = T(0), imv = T(1);
+        if (FAST && act) imv = ld1(ima, q);
         T a1e = T(0), b12v = T(0), b13v = T(0), a1h = T(0), b12h = T(0), b13h = T(0);
         T a3f = T(0), a3b = T(0), b31v = T(0), b31b = T(0), b32v = T(0), b32b = T(0), rhv = T(0);
         // (ld1: arrays this launch reads once; a1, b12, b21, b31 and c' are
@@ -564,7 +584,10 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
             row(pk, j + 1, q0 - sk, Bp, hBp);
         }
 #if PLES_LINE_PF_ROWS > 0
-        if (act && j + PLES_LINE_PF_ROWS < j1) {
+        if (FAST) {
+            if (pfa && j + PLES_LINE_PF_ROWS < j1 && (lane < 15 || j + PLES_LINE_PF_ROWS + 1 < nj))
+                pf_l2(pfa, q + PLES_LINE_PF_ROWS * sj);
+        } else if (act && j + PLES_LINE_PF_ROWS < j1) {
             const unsigned qn = q + PLES_LINE_PF_ROWS * sj;
             pf_l2(c.a1, qn); pf_l2(c.b12, qn); pf_l2(c.b13, qn);
             pf_l2(c.a2, qn); pf_l2(c.b21, qn); pf_l2(c.b23, qn);
@@ -589,7 +612,7 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
                 f = noneigh ? T(0) : b23v * (Fp + F0 - Bp - B0);
                 if (!odd && !noneigh) f += b21v * (pen + pe - pwn - pw);
                 a = T(0);
-                im = T(1) / a2v;
+                im = FAST ? imv : T(1) / a2v;
                 tp = a2v * P0 - a2v * Pp;
                 if (a2v == T(0)) { im = T(1); f = T(0); tp = P0; }  // wall row above a solid cell
             }
@@ -598,7 +621,7 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
                 f = noneigh ? T(0) : -(b23s * (F0 + Fm - B0 - Bm));
                 if (!odd && !noneigh) f -= b21s * (pe + pes - pw - pws);
                 a = -a2s;
-                im = T(1) / (a2s - a * cps);
+                im = FAST ? imv : T(1) / (a2s - a * cps);
                 tp = a2s * P0 - a2s * Pm;
                 if (a2s == T(0)) { im = T(1); f = T(0); tp = P0; }  // wall row below a solid cell
             }
@@ -615,7 +638,7 @@ __device__ __forceinline__ void build_rows(const Geom& g, const Coef<T>& c, cons
             if (act) {
                 a = a2s;
                 const T b = -(a2v + a + a1e + a1w + a3f + a3b);
-                im = T(1) / (b - a * cps);
+                im = FAST ? imv : T(1) / (b - a * cps);
                 f = rhv;
                 tp = a * Pm + b * P0 + a2v * Pp;
                 if (b == T(0)) {  // solid cell of an immersed-boundary mask: identity row
@@ -937,11 +960,12 @@ __device__ __forceinline__ void store_pair(const Geom& g, float* p, int i, int j
 
 // Block coordinates: x the 64-line tile, y the plane of this k parity; 16
 // warps.  Shared memory: 3 arrays [ny+2][64] and the segment maps [4][16][32].
-template <bool ZIN>
+template <bool ZIN, bool FAST = false>
 __device__ __forceinline__ void k_line_relax_x2_blk(Geom g, Coef<float> c, const float* __restrict__ cpa,
                                                     const float* __restrict__ pin, const float* __restrict__ pk,
                                                     float* __restrict__ pout, const float* __restrict__ rh,
-                                                    float omega, int kpar, int zk, const Blk& B) {
+                                                    float omega, int kpar, int zk, const Blk& B,
+                                                    const float* __restrict__ ima = nullptr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nj = g.ny + 2;
     float* G = reinterpret_cast<float*>(smem_raw);
@@ -959,8 +983,8 @@ __device__ __forceinline__ void k_line_relax_x2_blk(Geom g, Coef<float> c, const
     const int L = 32 * (w >> 3) + lane;
     const int ib = i0 + L;
     const int colb = (L & 1) ? 32 + (L >> 1) : (L >> 1);
-    build_rows<float, true, ZIN, false, 64>(g, c, cpa, pin, pk, rh, omega, zk, ib, k, (ib & 1) != 0, G, AL, CP,
-                                             w & 7, 8, colb);
+    build_rows<float, true, ZIN, false, 64, FAST>(g, c, cpa, pin, pk, rh, omega, zk, ib, k, (ib & 1) != 0, G, AL,
+                                                   CP, w & 7, 8, colb, ima);
     // the lane's two lines in the solve phases: io = i0 + 2 lane (odd i,
     // column lane) and io + 1 (even i, column 32 + lane)
     const int io = i0 + 2 * lane;
@@ -978,6 +1002,15 @@ __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c,
                                                           float* __restrict__ pout, const float* __restrict__ rh,
                                                           float omega, int kpar, int zk) {
     k_line_relax_x2_blk<ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
+}
+// the same with the pivot reciprocals of ima and the lane-parallel prefetch
+template <bool ZIN>
+__global__ void __launch_bounds__(512, 2) k_line_relax_x2f(Geom g, Coef<float> c, const float* __restrict__ cpa,
+                                                           const float* __restrict__ ima,
+                                                           const float* __restrict__ pin, const float* __restrict__ pk,
+                                                           float* __restrict__ pout, const float* __restrict__ rh,
+                                                           float omega, int kpar, int zk) {
+    k_line_relax_x2_blk<ZIN, true>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk(), ima);
 }
 
 // ---------------------------------------------------------------------------

@@ -277,6 +277,22 @@ int dalloc(ples_mg_handle* h, void** p, size_t bytes) {
     return PLES_MG_OK;
 }
 
+// Several equally sized boxes in one allocation, box a starting a x (box
+// bytes rounded up to 128 + kArenaSkew) into it: arrays a kernel reads at the
+// same element offset then differ in their address bits below any power of
+// two, so they do not fall into the same L2 sets or memory channels (boxes
+// allocated one by one start on 2 MB boundaries).  Each box stays 128-byte
+// aligned.
+constexpr size_t kArenaSkew = 4096 + 128;
+int dalloc_arena(ples_mg_handle* h, size_t bytes_each, int count, void** out[]) {
+    const size_t stride = (bytes_each + 127) / 128 * 128 + kArenaSkew;
+    void* base = nullptr;
+    int rc = dalloc(h, &base, stride * (size_t)count);
+    if (rc) return rc;
+    for (int a = 0; a < count; ++a) *out[a] = static_cast<char*>(base) + stride * (size_t)a;
+    return PLES_MG_OK;
+}
+
 template <typename T>
 int alloc_coef(ples_mg_handle* h, const Geom& g, Coef<T>& c) {
     T** f[9] = {&c.a1, &c.b12, &c.b13, &c.a2, &c.b21, &c.b23, &c.a3, &c.b31, &c.b32};
@@ -346,6 +362,8 @@ int set_x2_smem_attr(ples_mg_handle* h, size_t smem) {
     current = smem;
     CK(cudaFuncSetAttribute(k_line_relax_x2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_x2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_x2f<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_x2f<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_p2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_p2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
@@ -548,9 +566,10 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
             if (x2) {  // zebra on 64-line tiles
                 dim3 grd((L.g.nx + 63) / 64, (L.g.nz + 1) / 2);
                 const size_t sm = line_smem_x2(L.g);
-                auto kern = zin ? k_line_relax_x2<true> : k_line_relax_x2<false>;
-                kern<<<grd, 512, sm, h->st>>>(L.g, c, cp, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
-                kern<<<grd, 512, sm, h->st>>>(L.g, c, cp, pin, pout, pout, (const T*)L.rh, om, 1, 0);
+                auto kern = zin ? k_line_relax_x2f<true> : k_line_relax_x2f<false>;
+                const float* im = (const float*)L.im;
+                kern<<<grd, 512, sm, h->st>>>(L.g, c, cp, im, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
+                kern<<<grd, 512, sm, h->st>>>(L.g, c, cp, im, pin, pout, pout, (const T*)L.rh, om, 1, 0);
                 h->launches += 2;
                 staged = true;
             }
@@ -1386,20 +1405,28 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
             L.has_cd = true;
         }
         if (mixed) {
-            if ((rc = alloc_coef(h, L.g, L.cf)) || (rc = scale_into(h, n, gr, L.cf))) { free_tmp(tmp); return rc; }
+            // the nine FP32 coefficient boxes, rh, c', 1/m and the two field
+            // buffers of the level in one staggered allocation
+            void** boxes[14] = {(void**)&L.cf.a1, (void**)&L.cf.b12, (void**)&L.cf.b13, (void**)&L.cf.a2,
+                                (void**)&L.cf.b21, (void**)&L.cf.b23, (void**)&L.cf.a3, (void**)&L.cf.b31,
+                                (void**)&L.cf.b32, &L.rh, &L.cp, &L.im, &L.p, &L.p2};
+            if ((rc = dalloc_arena(h, sizeof(float) * (size_t)L.g.n, 14, boxes)) ||
+                (rc = scale_into(h, n, gr, L.cf))) {
+                free_tmp(tmp);
+                return rc;
+            }
             if (h->masked) mask_coef(h, n, L.cf);
             L.has_cf = true;
         }
         CK(cudaStreamSynchronize(h->st));
         free_tmp(tmp);
         const size_t es = mixed ? sizeof(float) : sizeof(double);
-        if ((rc = dalloc(h, &L.p, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.p2, es * (size_t)L.g.n)) ||
-            (rc = dalloc(h, &L.rh, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.cp, es * (size_t)L.g.n)))
+        if (!mixed && ((rc = dalloc(h, &L.p, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.p2, es * (size_t)L.g.n)) ||
+                       (rc = dalloc(h, &L.rh, es * (size_t)L.g.n)) || (rc = dalloc(h, &L.cp, es * (size_t)L.g.n))))
             return rc;
         // the 64-line-tile forms: FP32 zebra with periodic x and z, nx even
         L.x2_ok = mixed && h->smoother == 0 && L.g.px && L.g.pz && L.g.nx % 2 == 0 && L.g.nz >= 2 &&
                   line_smem_x2(L.g) <= 227 * 1024;
-        if (L.x2_ok && (rc = dalloc(h, &L.im, sizeof(float) * (size_t)L.g.n))) return rc;
         dim3 lg((L.g.nx + 127) / 128, L.g.nz);
         if (mixed)
             k_line_lu<float><<<lg, 128, 0, h->st>>>(L.g, L.cf, (float*)L.cp, (float*)L.im);

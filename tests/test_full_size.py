@@ -22,8 +22,9 @@ C ABI (GPU, slow: each runs the CPU oracle on a grid of the benchmark).
 * the immersed-boundary channel 512x256x512 (32 seeded spheres): the masked
   restatement of the reference's fine-level system (oracle.masked) gives the
   device solution a relative residual <= 2e-10 and wall-row residuals at the
-  same level; at 64x32x64 with the same sphere distribution the device
-  solution is within 1e-8 of the masked oracle's exact (sparse direct) one.
+  same level; at 48x24x48 with the same sphere distribution the device
+  solution is within 1e-8 of the masked oracle's exact (sparse direct) one,
+  and at 64x32x64 its masked residual is at the same level.
 """
 import json
 import os
@@ -168,20 +169,30 @@ def test_ib_512x256x512_masked_residual_of_device_solution():
     assert np.linalg.norm(rw) / bn <= 2e-10
 
 
-def test_ib_64x32x64_sphere_distribution_against_sparse_direct():
+def test_ib_48x24x48_sphere_distribution_against_sparse_direct():
+    """The benchmark's sphere distribution on a grid the sparse-direct
+    oracle factors in about two minutes (the 64x32x64 system takes a quarter
+    of an hour: fill-in of the 3-D stencil), plus the masked residual of the
+    device solution at 64x32x64."""
     from oracle import masked as M
-    nx, ny, nz = 64, 32, 64
-    x, y, z = S.wavy_channel_grid(nx, ny, nz, 0.1, 3.0)
-    rhs = S.divergence_rhs(nx, ny, nz, seed=4)
-    solid = S.sphere_mask(x, y, z, n=32, rmin=0.05, rmax=0.2, seed=11)
-    assert solid.any()
-    ref = M.solve(Oracle(x, y, z, islor=1, nlevmax=1), rhs, solid)
-    fl = ~solid
-    for prec in ("mixed", "fp64"):
-        with mg.Multigrid(x, y, z, precision=prec, solid=solid) as m:
-            fi, st = m.solve(rhs, rel_tol=1e-10)
-        assert st["status"] == mg.OK, st
-        p = fi[1:-1, 1:-1, 1:-1]
-        p = np.where(fl, p - p[fl].mean(), 0.0)
-        l2, mx = _rel(p, ref)
-        assert l2 <= SOL_TOL and mx <= SOL_TOL, (prec, l2, mx)
+    for nx, ny, nz in ((48, 24, 48), (64, 32, 64)):
+        x, y, z = S.wavy_channel_grid(nx, ny, nz, 0.1, 3.0)
+        rhs = S.divergence_rhs(nx, ny, nz, seed=4)
+        solid = S.sphere_mask(x, y, z, n=32, rmin=0.05, rmax=0.2, seed=11)
+        assert solid.any()
+        orc = Oracle(x, y, z, islor=1, nlevmax=1)
+        ref = M.solve(orc, rhs, solid) if nx == 48 else None
+        fl = ~solid
+        for prec in ("mixed", "fp64"):
+            with mg.Multigrid(x, y, z, precision=prec, solid=solid) as m:
+                fi, st = m.solve(rhs, rel_tol=1e-10)
+            assert st["status"] == mg.OK, st
+            if ref is not None:
+                p = fi[1:-1, 1:-1, 1:-1]
+                p = np.where(fl, p - p[fl].mean(), 0.0)
+                l2, mx = _rel(p, ref)
+                assert l2 <= SOL_TOL and mx <= SOL_TOL, (nx, prec, l2, mx)
+            r, rw = M.residual(orc, fi, rhs, solid)
+            b = np.where(fl, rhs, 0.0)
+            bn = np.linalg.norm(np.where(fl, b - b[fl].mean(), 0.0))
+            assert np.linalg.norm(r) / bn <= 2e-10 and np.linalg.norm(rw) / bn <= 2e-10, (nx, prec)
