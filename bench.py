@@ -44,17 +44,19 @@ UNIT = "solves/s"
 # coefficients, write p (12 x 4 B)
 LINE_BYTES_PER_CELL = 48
 # DRAM bytes (read + written) of one level-1 sweep of the smoother, from one
-# ncu capture of `python bench.py --steps 1 --warmup 3 --fp64-steps 0
+# ncu capture (`ncu --set full --clock-control none -k regex:k_line_relax_x2f
+# -s 12 -c 2` of `python bench.py --steps 1 --warmup 3 --fp64-steps 0
 # --e2e-steps 0 --no-cpu-baseline --batch-steps 0 --serve-requests 0
-# --ib-steps 0` with dram__bytes_read.sum + dram__bytes_write.sum over the
+# --ib-steps 0`): dram__bytes_read.sum + dram__bytes_write.sum over the two
 # launches of one sweep; keyed by workload and the kernel that capture timed,
 # and reported only when the bench times that same kernel
 LINE_TRAFFIC = {
-    ("channel_256x128x256", "k_line_relax_x2"): 316386560 + 317648128,
+    ("channel_256x128x256", "k_line_relax_x2f"): 335541504 + 335393792,
 }
 # the level-1 smoother form (threads per CTA as ples_mg_set_line_threads
 # takes them) -> the kernel it launches
-LINE_KERNELS = {1024: "k_line_relax_x2", 512: "k_line_relax_w", 256: "k_line_relax", 128: "k_line_relax"}
+LINE_KERNELS = {2048: "k_line_relax_p2", 1024: "k_line_relax_x2f", 512: "k_line_relax_w", 256: "k_line_relax",
+                128: "k_line_relax"}
 
 
 def _workload_config(w):
