@@ -77,14 +77,14 @@ typedef struct {
                               reference's multigrid: solid cells are removed
                               from the system (Neumann at their faces); the
                               solution is 0 there and rhs, compatibility and
-                              mean refer to the fluid cells.  Not for batches. */
+                              mean refer to the fluid cells. */
     const int *tipo;       /* PLES's immersed-boundary cell types (0:jx+1,0:jy+1,
                               0:jz+1) (0 solid, 1 IB, >= 2 fluid), or NULL.  As
                               in multi with bodyforce = 1 (multigrid.f03:615-
                               631), the max-norm stop test (eps / max_residual)
                               then runs over the fluid cells only; the operator
                               is unchanged.  Also the input of
-                              ples_mg_potenziale_ibm.  Not for batches. */
+                              ples_mg_potenziale_ibm. */
     int freesurface;       /* multi's freesurface argument (multigrid.f03:48): 1 =
                               the top wall row takes the free-surface relation
                               of mul_boun_sndrcv (multigrid.f03:1188-1222) with
@@ -291,8 +291,9 @@ int ples_mg_get_line_threads(const ples_mg_handle *h, int level, int *threads);
 /* ---- many grids at once ------------------------------------------------
  * No counterpart in the reference, which solves one grid per run.  A batch
  * groups existing handles (mixed precision, zebra smoother, full
- * coarsening, nu_pre == nu_post, all on one device); each keeps its
- * resident hierarchy.  One outer iteration of all members is a captured
+ * coarsening, nu_pre == nu_post, periodic x and z, a dense coarsest level,
+ * all on one device; immersed-boundary masks and cell types allowed); each
+ * keeps its resident hierarchy.  One outer iteration of all members is a captured
  * CUDA graph of persistent step kernels that walk (member, level, tile)
  * queues; convergence is decided per member on the device, so members of
  * different sizes finish independently.  The stop rule is the relative one

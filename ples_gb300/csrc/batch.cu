@@ -70,10 +70,11 @@ struct TaskHead {
 struct GhostTask { TaskHead h; Geom g; double* p; };
 struct SumTask { TaskHead h; Geom g; const double* a; double* part; int squares; };
 struct RedTask { TaskHead h; int mode; const double* pa; const double* pb; long long n; double ncell; };
-struct AddTask { TaskHead h; Geom g; double* a; int box; int use_mean; };
+struct AddTask { TaskHead h; Geom g; double* a; int box; int use_mean; const uint8_t* solid; };
+struct ZeroTask { TaskHead h; Geom g; double* a; const uint8_t* solid; };
 struct WallCTask { TaskHead h; Geom g; Coef<double> c; const double* p; double* w; };
 struct WallSTask { TaskHead h; Geom g; double* p; const double* w; };
-struct RoutTask { TaskHead h; Geom g; Coef<double> c; const double* x; const double* b; float* rin; double* psq; double* pmax; };
+struct RoutTask { TaskHead h; Geom g; Coef<double> c; const double* x; const double* b; float* rin; double* psq; double* pmax; const uint8_t* tipo; };
 struct LineTask { TaskHead h; Geom g; Coef<float> c; const float* cp; const float* pin; const float* pk; float* pout; const float* rh; float omega; int kpar; int zk; int wide; };
 struct RRTask { TaskHead h; Geom gf, gc; Coef<float> c; const float* p; const float* rh; float* rhc; int rx, ry, rz; };
 struct DenseTask { TaskHead h; Geom g; const float* S; const float* rh; float* p; };
@@ -130,8 +131,16 @@ __global__ void kb_add(WALK_ARGS) {
     walk(t, n, total, ctr, st, ph, [st](const AddTask& k, const Blk& B) {
         const InstState& S = st[k.h.inst];
         const double v = -(k.use_mean ? S.mean : S.shift);
-        if (k.box) k_add_box_blk(k.g, k.a, v, nullptr, B);
-        else k_add_interior_blk(k.g, k.a, v, nullptr, B);
+        if (k.box) k_add_box_blk(k.g, k.a, v, k.solid, B);
+        else k_add_interior_blk(k.g, k.a, v, k.solid, B);
+    });
+}
+// a field set to zero on the solid cells of a member's immersed-boundary mask
+template <class T>
+__global__ void kb_zero(WALK_ARGS) {
+    walk(t, n, total, ctr, st, ph, [](const ZeroTask& k, const Blk& B) {
+        for (long long q = (long long)B.x * blockDim.x + threadIdx.x; q < k.g.n; q += (long long)B.gx * blockDim.x)
+            if (k.solid[q]) k.a[q] = 0.0;
     });
 }
 template <class T>
@@ -147,7 +156,7 @@ __global__ void kb_walls(WALK_ARGS) {
 template <class T>
 __global__ void __launch_bounds__(256) kb_rout(WALK_ARGS) {
     walk(t, n, total, ctr, st, ph, [](const RoutTask& k, const Blk& B) {
-        k_resid_outer2_blk<float, 8>(k.g, k.c, k.x, k.b, k.rin, k.psq, k.pmax, B);
+        k_resid_outer2_blk<float, 8>(k.g, k.c, k.x, k.b, k.rin, k.psq, k.pmax, B, k.tipo);
     });
 }
 template <class T, bool ZIN>
@@ -254,7 +263,8 @@ dim3 cgrid(const Geom& g, int ghost) {
     return ghost ? dim3((g.nx + 2 + 31) / 32, (g.ny + 2 + 3) / 4, g.nz + 2) : dim3((g.nx + 31) / 32, (g.ny + 3) / 4, g.nz);
 }
 
-enum Kind { K_GHOST, K_SUM, K_RED, K_ADD, K_WALLC, K_WALLS, K_ROUT, K_LINE0, K_LINE1, K_RR, K_DENSE, K_PROL, K_UPD };
+enum Kind { K_GHOST, K_SUM, K_RED, K_ADD, K_WALLC, K_WALLS, K_ROUT, K_LINE0, K_LINE1, K_RR, K_DENSE, K_PROL, K_UPD,
+            K_ZERO };
 
 struct Step {
     int kind, phase;
@@ -390,7 +400,7 @@ int build_steps(ples_mg_batch* b) {
             RedTask t{};
             t.h.inst = i;
             t.mode = mode;
-            t.ncell = (double)g.nx * g.ny * g.nz;
+            t.ncell = h->masked ? (double)h->nfluid : (double)g.nx * g.ny * g.nz;
             if (src == 0) {
                 const dim3 r = red_grid2(g);
                 t.pa = h->part_a;
@@ -415,7 +425,22 @@ int build_steps(ples_mg_batch* b) {
             t.a = on_x ? h->x : h->b;
             t.box = on_x;
             t.use_mean = on_x;
+            t.solid = h->masked ? h->mask[0] : nullptr;
             B.add(t, on_x ? box_grid2(t.g) : dim3((t.g.nx + 31) / 32, (t.g.ny + 3) / 4, t.g.nz));
+        }
+        B.end();
+    };
+    auto zero_step = [&](int phase, bool on_x) {  // masked members: the field vanishes on solid cells
+        B.begin<ZeroTask>(K_ZERO, phase);
+        for (int i = 0; i < nm; ++i) {
+            ples_mg_handle* h = b->mem[i];
+            if (!h->masked) continue;
+            ZeroTask t{};
+            t.h.inst = i;
+            t.g = h->L[0].g;
+            t.a = on_x ? h->x : h->b;
+            t.solid = h->mask[0];
+            B.add(t, dim3((unsigned)std::min<long long>((t.g.n + 255) / 256, 4096), 1, 1));
         }
         B.end();
     };
@@ -458,7 +483,10 @@ int build_steps(ples_mg_batch* b) {
         }
     };
 
-    // ---- prologue: periodic ghosts of fi, compatibility projection, |b|
+    // ---- prologue: solid cells of masked members zeroed, periodic ghosts of
+    // fi, compatibility projection, |b|
+    zero_step(PH_PRO, true);
+    zero_step(PH_PRO, false);
     B.begin<GhostTask>(K_GHOST, PH_PRO);
     for (int i = 0; i < nm; ++i) {
         ples_mg_handle* h = b->mem[i];
@@ -516,6 +544,7 @@ int build_steps(ples_mg_batch* b) {
         t.rin = (float*)h->L[0].rh;
         t.psq = h->part_a;
         t.pmax = h->part_b;
+        t.tipo = h->tipo;
         B.add(t, rout_grid(t.g));
     }
     B.end();
@@ -592,7 +621,9 @@ int build_steps(ples_mg_batch* b) {
     }
     B.end();
 
-    // ---- epilogue: zero mean, then done
+    // ---- epilogue: solid cells reset (the prolongation may have touched
+    // them), zero mean over the fluid cells, then done
+    zero_step(PH_EPI, true);
     sum_step(PH_EPI, true, 0);
     red_step(PH_EPI, RED_MEAN, 0);
     add_step(PH_EPI, true);
@@ -659,6 +690,7 @@ int record_steps(ples_mg_batch* b) {
             case K_DENSE: rc = launch_step<DenseTask>(b, s, i, kb_dense<DenseTask>, b1, b->smem_dense); break;
             case K_PROL: rc = launch_step<ProlTask>(b, s, i, kb_prol<ProlTask>, b2, 0); break;
             case K_UPD: rc = launch_step<UpdTask>(b, s, i, kb_upd<UpdTask>, b2, 0); break;
+            case K_ZERO: rc = launch_step<ZeroTask>(b, s, i, kb_zero<ZeroTask>, b1, 0); break;
         }
         if (rc) return rc;
     }
@@ -675,9 +707,7 @@ int batch_create(ples_mg_handle* const* members, int n, ples_mg_batch* b) {
             return bfail(b, PLES_MG_BAD_ARG,
                          "member %d: batched solves need mixed precision, the zebra smoother and full coarsening", i);
         if (!h->coarse_S) return bfail(b, PLES_MG_BAD_ARG, "member %d: coarsest level too large for the dense solve", i);
-        if (h->masked) return bfail(b, PLES_MG_BAD_ARG, "member %d: immersed-boundary masks are not batched", i);
         if (h->walls_xz) return bfail(b, PLES_MG_BAD_ARG, "member %d: x or z walls are not batched", i);
-        if (h->tipo) return bfail(b, PLES_MG_BAD_ARG, "member %d: cell types (tipo) are not batched", i);
         if (h->nu_pre != h->nu_post)
             return bfail(b, PLES_MG_BAD_ARG, "member %d: batched solves need nu_pre == nu_post", i);
         for (int l = 1; l < h->nlev; ++l)

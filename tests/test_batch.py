@@ -80,6 +80,36 @@ def test_batch_rejects_unsupported_members(cases):
             mg.Batch([m])
 
 
+def test_batch_with_masked_and_typed_members():
+    """Members with an immersed-boundary mask and with PLES cell types in one
+    batch with a plain member: each batched result agrees with the same grid
+    solved alone within 1e-9 (the sums of the compatibility shift and the
+    mean are reduced in another order), the masked member's field vanishes
+    on its solid cells and the typed member's max residual is its fluid-cell
+    stop test (within 1e-2 of the single solve's: both are FP64 residuals of
+    ~1e-11 of slightly different converged fields)."""
+    dims = (32, 16, 32)
+    x, y, z = S.wavy_channel_grid(*dims, 0.08, 2.0)
+    solid = S.sphere_mask(x, y, z, n=6, rmin=0.3, rmax=0.5, seed=3)
+    tipo = np.full((dims[0] + 2, dims[1] + 2, dims[2] + 2), 2, dtype=np.int32, order="F")
+    tipo[8:14, 4:9, 10:18] = 0
+    rhs = [S.divergence_rhs(*dims, seed=s) for s in (41, 42, 43)]
+    opts = [dict(solid=solid), dict(tipo=tipo), {}]
+    members = [mg.Multigrid(x, y, z, **o) for o in opts]
+    try:
+        singles = [m.solve(r, rel_tol=REL_TOL) for m, r in zip(members, rhs)]
+        with mg.Batch(members) as b:
+            fis, sts = b.solve(rhs, rel_tol=REL_TOL)
+        for (fs, ss), fb, sb in zip(singles, fis, sts):
+            assert sb["status"] == mg.OK and ss["status"] == mg.OK and sb["rel_residual"] <= REL_TOL
+            assert np.abs(fb - fs).max() <= 1e-9 * np.abs(fs).max()
+        assert np.all(fis[0][1:-1, 1:-1, 1:-1][solid] == 0.0)
+        assert sts[1]["max_residual"] == pytest.approx(singles[1][1]["max_residual"], rel=1e-2)
+    finally:
+        for m in members:
+            m.close()
+
+
 def test_server_same_result_alone_and_in_the_mix(cases):
     # identical grids on separate handles, both starting from zero
     alone = [mg.Multigrid(*cases[1][:3])]
