@@ -520,8 +520,16 @@ def serve_leg(args, local):
                 "outer_iterations_mean": float(np.mean(outer))}
 
     full = run(args.serve_rate, args.serve_requests, 7)
-    rate2 = 0.7 * full["solves_per_s"]
-    light = run(rate2, max(32, int(rate2 * 2.0)), 8)
+    # offered rates below the throughput measured at the full rate: the
+    # highest one whose p99 stays within the bound is the capacity
+    p99_bound_ms = 250.0
+    sweep = {}
+    for seed, frac in ((8, 0.7), (9, 0.5), (10, 0.9)):
+        rate = frac * full["solves_per_s"]
+        sweep[frac] = run(rate, max(32, int(rate * 2.0)), seed)
+    light = sweep[0.7]
+    ok = [v for v in sweep.values() if v["p99_ms"] <= p99_bound_ms]
+    capacity = max(ok, key=lambda v: v["offered_rate"]) if ok else None
     srv.close()
     for h in handles:
         h.close()
@@ -529,6 +537,12 @@ def serve_leg(args, local):
            "cells_total": int(sum(w.cells for w in ms)), "hbm_budget_bytes": 150e9}
     out.update(full)
     out["at_70pct_throughput"] = light
+    out["rate_sweep"] = [{"fraction_of_throughput": f, "offered_rate": v["offered_rate"], "p50_ms": v["p50_ms"],
+                          "p99_ms": v["p99_ms"], "p999_ms": v["p999_ms"], "solves_per_s": v["solves_per_s"]}
+                         for f, v in sorted(sweep.items())]
+    out["capacity"] = ({"p99_bound_ms": p99_bound_ms, "offered_rate": capacity["offered_rate"],
+                        "p50_ms": capacity["p50_ms"], "p99_ms": capacity["p99_ms"]}
+                       if capacity else {"p99_bound_ms": p99_bound_ms, "offered_rate": None})
     out["note"] = "latency includes queueing whenever the offered rate exceeds the throughput"
     return out
 
