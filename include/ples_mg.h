@@ -270,9 +270,14 @@ typedef struct {
 } ples_mg_tuning;
 int ples_mg_autotune(ples_mg_handle *h, const double *rhs, ples_mg_tuning *out);
 /* Set the form of the eta-line smoother at one level (1-based), as the
- * autotuner does: 128, 256 or 512 threads per CTA on 32-line tiles, or 1024
+ * autotuner does: 128, 256 or 512 threads per CTA on 32-line tiles, 1024
  * for the 64-line-tile form (512 threads; mixed precision, zebra smoother,
- * x and z periodic, nx of the level even, nz >= 2).  No counterpart in the
+ * x and z periodic, nx of the level even, nz >= 2), 2048 for the same tiles
+ * with rows built two lines per thread (256 threads), or 4096 for the
+ * 64-line tiles with both k parities of a sweep in one launch (an even-k
+ * tile starts once the odd planes either side of it are stored; its wait is
+ * bounded by ples_mg_set_wait_limit, and one that runs out ends the solve
+ * with PLES_MG_DEVICE_TIMEOUT).  No counterpart in the
  * reference (its sweeps are scalar loops, multigrid.f03:1939-2290).  BAD_ARG
  * for another value, a form that does not apply at that level or whose
  * shared memory does not fit. */

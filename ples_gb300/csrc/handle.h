@@ -36,7 +36,8 @@ struct LevelData {
     // form of the eta-line smoother: 128, 256 or 512 threads on 32-line
     // tiles, 1024 for the 64-line-tile form (512 threads, k_line_relax_x2),
     // 2048 for the 64-line tiles with the pair build (256 threads,
-    // k_line_relax_p2); autotuned
+    // k_line_relax_p2), 4096 for the 64-line tiles with both k parities in
+    // one launch (512 threads, k_line_relax_x2m); autotuned
     int line_threads = 256;
     bool x2_ok = false;  // the 64-line-tile form applies (FP32, x and z periodic, nx even, nz >= 2)
     bool tma = false;
@@ -61,6 +62,7 @@ struct ples_mg_handle {
     long long npart = 0;
     double* red = nullptr;                               // 2 doubles on the device (+ dflag)
     int* dflag = nullptr;                                // bounded-wait error flag, inside red
+    int* x2sync = nullptr;                               // tickets and plane counters of k_line_relax_x2m (nz + 3)
     unsigned wait_polls = ples::kSpinLimit;              // polls of a bounded device wait before it gives up
     double* h_red = nullptr;                             // pinned host copy
     double* norm_scratch = nullptr;  // device address of the library's fixed residual scratch (this device)

@@ -107,6 +107,19 @@ __device__ __forceinline__ T ld1(const T* p, unsigned q) {
 #endif
 }
 
+// Every spin-wait on the device is bounded: it gives up after kSpinLimit
+// polls (or fewer, when the handle's wait limit says so) or kWaitNs of wall
+// time, whichever comes first.
+constexpr unsigned kSpinLimit = 1u << 26;              // polls of one wait at most
+constexpr unsigned long long kWaitNs = 2000000000ull;  // and 2 s of wall time
+
+// nanoseconds of the GPU's global timer
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // element offset of (i,j,k) in 32 bits: a box has fewer than 2^31 elements
 // (checked when a handle is created), so kernels that issue many loads per
 // cell form each address with one 32x32->64 multiply-add
@@ -1003,6 +1016,101 @@ __global__ void __launch_bounds__(512, 2) k_line_relax_x2(Geom g, Coef<float> c,
                                                           float omega, int kpar, int zk) {
     k_line_relax_x2_blk<ZIN>(g, c, cpa, pin, pk, pout, rh, omega, kpar, zk, hw_blk());
 }
+// a relaxed load of a counter that other CTAs increment (no L1 invalidation
+// per poll, unlike an acquire load: the CTA sharing the SM keeps its cache)
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Thread 0 of an even-plane CTA: wait until the counters of the odd planes
+// kb and kf reach ntx (relaxed polls with a short sleep, then one acquire
+// fence), at most `polls` polls and kWaitNs; 0 and *err = 1 when it gives up.
+// Not inlined: its registers are not held across the sweep that follows.
+static __device__ __noinline__ int wait_odd_planes(const int* cnt, int kb, int kf, int ntx, unsigned polls, int* err) {
+    unsigned long long t0 = 0;
+    for (unsigned it = 0;; ++it) {
+        if (ld_relaxed_gpu(cnt + kb) >= ntx && ld_relaxed_gpu(cnt + kf) >= ntx) {
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            return 1;
+        }
+        const unsigned long long tn = global_ns();
+        if (t0 == 0) t0 = tn;
+        if (it >= polls || tn - t0 > kWaitNs) {
+            atomicExch(err, 1);
+            return 0;
+        }
+        __nanosleep(128);
+    }
+}
+
+// Thread 0 after the CTA's barrier that follows its stores: release the
+// tile of odd plane k (k = 0: none), then count the CTA as finished; true
+// for the last CTA of the launch.  The release is cumulative over the
+// barrier, so it publishes the stores of every thread of the CTA; the
+// acquire-release count orders it before the last CTA's reset.
+static __device__ __noinline__ int finish_tile(int* sync, int k, int nblocks) {
+    if (k > 0) asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(sync + 2 + k) : "memory");
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(sync + 1) : "memory");
+    return old == nblocks - 1;
+}
+
+// Both k parities of one zebra sweep in a single launch (64-line tiles, the
+// FAST row build), 2 ntx ceil(nz/2) CTAs in one dimension.  Each CTA takes a
+// ticket from sync[0]: tickets below ntx ceil(nz/2) are the tiles of the
+// odd planes (the first launch of the two-launch sweep), the rest those of
+// the even planes.  An even-plane tile needs the new values of the odd
+// planes k-1 and k+1 (plane 1 for k = nz, whose ghost image it reads): its
+// first thread waits (wait_odd_planes) until their counters sync[2 + k']
+// reach ntx, each odd-plane CTA adding one after its stores (finish_tile).
+// A ticket is only ever held by a resident CTA and odd-plane CTAs wait for
+// nothing, so every wait ends; it is bounded all the same, after which the
+// CTA sets *err and leaves without writing.  Even-plane CTAs read the odd
+// planes only once they are complete and no CTA rewrites them; odd-plane
+// CTAs read only pin.  The last CTA to finish (sync[1] counts them) zeroes
+// sync[0 .. nz+2] for the next launch.  Same arithmetic as the two launches.
+template <bool ZIN>
+__global__ void __launch_bounds__(512, 2) k_line_relax_x2m(Geom g, Coef<float> c, const float* __restrict__ cpa,
+                                                           const float* __restrict__ ima,
+                                                           const float* __restrict__ pin, float* __restrict__ pout,
+                                                           const float* __restrict__ rh, float omega, int zk0,
+                                                           int* __restrict__ sync, int* __restrict__ err,
+                                                           unsigned polls) {
+    __shared__ int s_ticket, s_ok;
+    if (threadIdx.x == 0) s_ticket = atomicAdd(sync, 1);
+    __syncthreads();
+    const int ntx = (g.nx + 63) / 64, np0 = (g.nz + 1) / 2;
+    const int t = s_ticket;
+    const int kpar = t >= ntx * np0 ? 1 : 0;
+    const int u = kpar ? t - ntx * np0 : t;
+    Blk B;
+    B.gx = ntx;
+    B.gy = np0;
+    B.gz = 1;
+    B.x = u % ntx;
+    B.y = u / ntx;
+    B.z = 0;
+    const int k = 2 * B.y + 1 + kpar;
+    if (threadIdx.x == 0)
+        s_ok = kpar && k <= g.nz ? wait_odd_planes(sync + 2, k - 1, k + 1 <= g.nz ? k + 1 : 1, ntx, polls, err) : 1;
+    __syncthreads();
+    if (s_ok && k <= g.nz)
+        k_line_relax_x2_blk<ZIN, true>(g, c, cpa, pin, kpar ? pout : pin, pout, rh, omega, kpar, kpar ? 0 : zk0, B,
+                                       ima);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // the ticket again from shared memory: nothing of it stays live across the sweep
+        const int t2 = *(volatile int*)&s_ticket;
+        const int k2 = t2 < ntx * np0 ? 2 * (t2 / ntx) + 1 : 0;
+        s_ok = finish_tile(sync, k2 <= g.nz ? k2 : 0, (int)gridDim.x);
+    }
+    __syncthreads();
+    if (s_ok)  // the last CTA: no other CTA touches the counters any more
+        for (int q = threadIdx.x; q < g.nz + 3; q += blockDim.x) sync[q] = 0;
+}
+
 // the same with the pivot reciprocals of ima and the lane-parallel prefetch
 template <bool ZIN>
 __global__ void __launch_bounds__(512, 2) k_line_relax_x2f(Geom g, Coef<float> c, const float* __restrict__ cpa,

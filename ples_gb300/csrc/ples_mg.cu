@@ -366,6 +366,8 @@ int set_x2_smem_attr(ples_mg_handle* h, size_t smem) {
     CK(cudaFuncSetAttribute(k_line_relax_x2f<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_p2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_line_relax_p2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_x2m<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_line_relax_x2m<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return 0;
 }
 
@@ -517,6 +519,7 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
     const T om = T(h->omega);
     const bool x2 = std::is_same<T, float>::value && h->smoother == 0 && L.line_threads == 1024 && L.x2_ok;
     const bool p2 = std::is_same<T, float>::value && h->smoother == 0 && L.line_threads == 2048 && L.x2_ok;
+    const bool m2 = std::is_same<T, float>::value && h->smoother == 0 && L.line_threads == 4096 && L.x2_ok;
     const int nt = h->smoother == 1 ? std::min(L.line_threads, 256) : std::min(L.line_threads, 512);
     const size_t smem = line_smem<T>(L.g, nt);
     const T* cp = (const T*)L.cp;
@@ -559,6 +562,17 @@ void smooth(ples_mg_handle* h, LevelData& L, int nu, int level, bool zero) {
                 kern<<<grd, 256, sm, h->st>>>(L.g, c, cp, im, pin, pin, pout, (const T*)L.rh, om, 0, zin ? 1 : 0);
                 kern<<<grd, 256, sm, h->st>>>(L.g, c, cp, im, pin, pout, pout, (const T*)L.rh, om, 1, 0);
                 h->launches += 2;
+                staged = true;
+            }
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            if (m2) {  // zebra on 64-line tiles, both k parities in one launch
+                const int nb = 2 * ((L.g.nx + 63) / 64) * ((L.g.nz + 1) / 2);
+                const size_t sm = line_smem_x2(L.g);
+                auto kern = zin ? k_line_relax_x2m<true> : k_line_relax_x2m<false>;
+                kern<<<nb, 512, sm, h->st>>>(L.g, c, cp, (const float*)L.im, pin, pout, (const T*)L.rh, om,
+                                             zin ? 1 : 0, h->x2sync, h->dflag, h->wait_polls);
+                ++h->launches;
                 staged = true;
             }
         }
@@ -659,7 +673,7 @@ int reduce_to_host(ples_mg_handle* h, const double* a, const double* bmax, long 
     std::memcpy(&flag, h->h_red + 4, sizeof flag);
     if (flag) {
         CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
-        return fail(h, PLES_MG_DEVICE_TIMEOUT, "a staged transfer of the line smoother did not complete");
+        return fail(h, PLES_MG_DEVICE_TIMEOUT, "a bounded wait of the line smoother ran out");
     }
     return PLES_MG_OK;
 }
@@ -860,7 +874,7 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
         std::memcpy(&flag, h->h_red + 4, sizeof flag);
         if (flag) {
             CK(cudaMemsetAsync(h->dflag, 0, sizeof(int), h->st));
-            return fail(h, PLES_MG_DEVICE_TIMEOUT, "a staged transfer of the line smoother did not complete");
+            return fail(h, PLES_MG_DEVICE_TIMEOUT, "a bounded wait of the line smoother ran out");
         }
         rel = std::sqrt(r2[0]) / bnorm;
         rmax = r2[1];
@@ -1493,6 +1507,8 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         (rc = dalloc(h, (void**)&h->part_b, 8 * (size_t)h->npart)) || (rc = dalloc(h, (void**)&h->red, 64)))
         return rc;
     h->dflag = reinterpret_cast<int*>(h->red + 4);
+    if ((rc = dalloc(h, (void**)&h->x2sync, sizeof(int) * ((size_t)g.nz + 3)))) return rc;
+    CK(cudaMemsetAsync(h->x2sync, 0, sizeof(int) * ((size_t)g.nz + 3), h->st));
     CK(cudaMemsetAsync(h->red, 0, 64, h->st));
     CK(cudaMallocHost((void**)&h->h_red, 64));
     const size_t nfi = (size_t)(jx + 2) * (jy + 2) * (jz + 2), nrh = (size_t)jx * jy * jz;
@@ -2211,13 +2227,13 @@ int ples_mg_set_line_threads(ples_mg_handle* h, int level, int threads) {
     LevelData& L = h->L[level - 1];
     const bool mixed = h->d.precision == PLES_MG_PREC_MIXED;
     size_t need = 0;
-    if (threads == 1024 || threads == 2048) {
+    if (threads == 1024 || threads == 2048 || threads == 4096) {
         if (!L.x2_ok) return fail(h, PLES_MG_BAD_ARG, "the 64-line-tile smoother does not apply at level %d", level);
         need = line_smem_x2(L.g);
     } else if (threads == 128 || threads == 256 || threads == 512) {
         need = mixed ? line_smem<float>(L.g, threads) : line_smem<double>(L.g, threads);
     } else {
-        return fail(h, PLES_MG_BAD_ARG, "smoother form %d is not 128, 256, 512, 1024 or 2048", threads);
+        return fail(h, PLES_MG_BAD_ARG, "smoother form %d is not 128, 256, 512, 1024, 2048 or 4096", threads);
     }
     if (need > 227 * 1024) return fail(h, PLES_MG_BAD_ARG, "smoother form %d needs %zu B of shared memory", threads, need);
     L.line_threads = threads;
@@ -2349,6 +2365,9 @@ int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) 
         for (int n = 0; n < nsmooth; ++n) {
             double best = 1e300;
             int bt = h->L[n].line_threads;
+            // (form 4096, both k parities in one launch, measured slower
+            // than 1024 on GB300: 223 vs 212 us per 256x128x256 sweep, 62
+            // vs 44 at 128x64x128; not a candidate)
             for (int t : {128, 256, 512, 1024, 2048}) {
                 const LevelData& Ln = h->L[n];
                 if (t >= 1024 && !Ln.x2_ok) continue;

@@ -13,16 +13,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "mg_device.cuh"  // kSpinLimit, kWaitNs, global_ns
+
 namespace ples {
-
-constexpr unsigned kSpinLimit = 1u << 26;          // polls of one wait at most
-constexpr unsigned long long kWaitNs = 2000000000ull;  // and 2 s of wall time
-
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);

@@ -352,7 +352,9 @@ class Multigrid:
 
     def set_line_threads(self, level, threads):
         """Smoother form at one level (1-based): 128, 256 or 512 threads on
-        32-line tiles, or 1024 for the 64-line tiles (ples_mg_set_line_threads)."""
+        32-line tiles, 1024 for the 64-line tiles, 2048 for the same tiles
+        with rows built two lines per thread, 4096 for the 64-line tiles
+        with both k parities in one launch (ples_mg_set_line_threads)."""
         self._check(self._L.ples_mg_set_line_threads(self._h, level, threads))
 
     def set_surface_pressure(self, next_prs=None):

@@ -317,7 +317,7 @@ def test_pair_build_smoother_matches_single_line_build(dims):
     rhs = S.divergence_rhs(*dims, seed=5)
     with mg.Multigrid(x, y, z) as m:
         forms = {}
-        for form in (1024, 2048):
+        for form in (1024, 2048, 4096):
             set_at = []
             for lev in range(1, m.nlevel + 1):
                 try:
@@ -332,3 +332,8 @@ def test_pair_build_smoother_matches_single_line_build(dims):
     assert s1["status"] == mg.OK and s2["status"] == mg.OK
     assert s1["outer_iterations"] == s2["outer_iterations"]
     assert np.abs(f1 - f2).max() <= 1e-9 * np.abs(f1).max()
+    # both k parities in one launch (form 4096): the same arithmetic as the
+    # two launches of form 1024, on the same inputs: bit for bit
+    f4, s4 = forms[4096]
+    assert s4["status"] == mg.OK and s4["outer_iterations"] == s1["outer_iterations"]
+    np.testing.assert_array_equal(f4, f1)
