@@ -36,7 +36,10 @@ enum {
 /* inner-solve precision */
 enum {
     PLES_MG_PREC_FP64 = 0,  /* plain: every kernel in FP64                          */
-    PLES_MG_PREC_MIXED = 1  /* FP32 V-cycle inside an FP64 defect-correction loop   */
+    PLES_MG_PREC_MIXED = 1, /* FP32 V-cycle inside an FP64 defect-correction loop   */
+    PLES_MG_PREC_OUTER = 2  /* ples_mg_apply_residual only: the solver's own outer
+                               residual of level 1 (double-float products on a
+                               mixed handle, FP64 on an FP64 one)               */
 };
 
 /* layout of the node coordinates in the descriptor */
@@ -165,7 +168,8 @@ int ples_mg_level_dims(const ples_mg_handle *h, int level, int *nx, int *ny,
 int ples_mg_get_metric(ples_mg_handle *h, int level, int which, double *out);
 /* rh1 = L_n(pr) - rh on the device (resid_sndrcv.f03:2-156);
  * pr (0:nx+1,0:ny+1,0:nz+1), rh/out (1:nx,1:ny,1:nz).  precision selects
- * the FP64 or the FP32 kernel. */
+ * the FP64 or the FP32 kernel, or (level 1) PLES_MG_PREC_OUTER the kernel
+ * the solve's stop test and defect correction use. */
 int ples_mg_apply_residual(ples_mg_handle *h, int level, const double *pr,
                            const double *rh, double *out, int precision);
 /* Ghost layer of pr at level `level` driven to the fixed point of the

@@ -30,7 +30,8 @@ struct LevelData {
     void* im = nullptr;          // pivot reciprocals 1/m of that operator (FP32 box, 64-line-tile levels)
     ples::Coef<float> cf{};             // FP32 scaled coefficients (mixed)
     ples::Coef<double> cd{};            // FP64 scaled coefficients (level 1 always; all levels in FP64 mode)
-    bool has_cf = false, has_cd = false;
+    ples::Coef<float2> cs{};            // the FP64 ones split into double-floats x 2^oc (level 1, mixed)
+    bool has_cf = false, has_cd = false, has_cs = false;
     // TMA-staged zebra smoother (FP32): tensor maps of this level's fields;
     // pA/pB are the buffers behind maps.pA/pB (p and p2 swap every sweep)
     // form of the eta-line smoother: 128, 256 or 512 threads on 32-line
@@ -62,6 +63,8 @@ struct ples_mg_handle {
     long long npart = 0;
     double* red = nullptr;                               // 2 doubles on the device (+ dflag)
     int* dflag = nullptr;                                // bounded-wait error flag, inside red
+    int* dscale = nullptr;                               // ob, ox of the double-float residual (inside red)
+    int oc = 0;                                          // power-of-two scale of the split coefficients
     int* x2sync = nullptr;                               // tickets and plane counters of k_line_relax_x2m (nz + 3)
     unsigned wait_polls = ples::kSpinLimit;              // polls of a bounded device wait before it gives up
     double* h_red = nullptr;                             // pinned host copy

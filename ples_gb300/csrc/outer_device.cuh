@@ -3,6 +3,7 @@
 // by the single-grid solver (ples_mg.cu) and the batched engine (batch.cu).
 // Each body takes its block coordinates (Blk) explicitly.
 #pragma once
+#include "dfloat.cuh"
 #include "mg_device.cuh"
 
 namespace ples {
@@ -149,6 +150,145 @@ __device__ __forceinline__ void k_resid_outer2_blk(Geom g, Coef<double> c, const
         pmax[blk] = m;
     }
 }
+// The same residual with the products and sums in double-float on the FP32
+// pipe (dfloat.cuh): the FP64 pipe takes only the differences of x, which
+// are formed in FP64 as above (the same rounding) and split into double-
+// floats on the bits.  The coefficients come pre-split (cs: head and tail,
+// times 2^oc); the differences are split times 2^ox and b times 2^ob, with
+// ob = ox + oc, so every term and r itself are b's scale times 2^ob, near 1.
+// The terms are products of a coefficient and a difference, so they are
+// carried with about 2^-47 of their own size, against about 2^-53 in FP64:
+// the residual agrees with the FP64 kernel's to a few units of 2^-47 of its
+// largest terms.  rin = r in Ti; the partial sums of squares and maxima are
+// taken in float on the scaled r and returned in FP64, unscaled.  sc[0] =
+// ob and sc[1] = ox are read from device memory, so one captured graph
+// serves any scaling.
+template <typename Ti, int KC>
+__device__ __forceinline__ void k_resid_outer2_df_blk(Geom g, Coef<float2> cs, const double* __restrict__ x,
+                                                      const double* __restrict__ b, Ti* __restrict__ rin,
+                                                      double* __restrict__ psq, double* __restrict__ pmax,
+                                                      const Blk& B, const uint8_t* __restrict__ tipo,
+                                                      const int* __restrict__ sc) {
+    __shared__ dfl sN[2][8][32], sDx[2][8][32], sDz[2][8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int i = B.x * 32 + tx + 1, j = B.y * 8 + ty + 1;
+    const int k0 = B.z * KC + 1, k1 = min(k0 + KC - 1, g.nz);
+    const bool act = i <= g.nx && j <= g.ny;
+    const int ic = min(i, g.nx), jc = min(j, g.ny);  // keep idle threads' loads in the box
+    const long long sj = g.sj, sk = g.sk;
+    const int ob = sc[0], ox = sc[1];
+    auto D = [&](long long qa, long long qz) { return df_from_double(x[qa] - x[qz], ox); };
+    auto C = [&](const float2* a, long long qq) {
+        const float2 v = a[qq];
+        return dfl{v.x, v.y};
+    };
+    auto shd = [&](dfl v, int d) { return dfl{__shfl_down_sync(0xffffffffu, v.h, d), __shfl_down_sync(0xffffffffu, v.l, d)}; };
+    auto shu = [&](dfl v, int d) { return dfl{__shfl_up_sync(0xffffffffu, v.h, d), __shfl_up_sync(0xffffffffu, v.l, d)}; };
+    float s = 0.f, m = 0.f;
+    long long q = g.at(ic, jc, k0);
+    dfl Dx0 = D(q + 1, q - 1), Dy0 = D(q + sj, q - sj), Dz0 = D(q + sk, q - sk);
+    dfl fB;
+    {
+        const long long qb = q - sk;
+        const dfl DxB = D(qb + 1, qb - 1), DyB = D(qb + sj, qb - sj);
+        fB = df_dot3(C(cs.a3, qb), D(q, qb), C(cs.b31, qb), df_add(Dx0, DxB), C(cs.b32, qb), df_add(Dy0, DyB));
+    }
+    for (int k = k0; k <= k1; ++k) {
+        q = g.at(ic, jc, k);
+        const int buf = k & 1;
+        sDx[buf][ty][tx] = Dx0;
+        sDz[buf][ty][tx] = Dz0;
+        const long long qf = q + sk;
+        const dfl Dx1 = D(qf + 1, qf - 1), Dy1 = D(qf + sj, qf - sj);
+        const dfl Dz1 = k < k1 ? D(qf + sk, q) : dfl{0.f, 0.f};
+        dfl DyE = shd(Dy0, 1), DzE = shd(Dz0, 1);
+        if (tx == 31 || i + 1 > g.nx) {
+            DyE = D(q + 1 + sj, q + 1 - sj);
+            DzE = D(q + 1 + sk, q + 1 - sk);
+        }
+        const dfl fE = df_dot3(C(cs.a1, q), D(q + 1, q), C(cs.b12, q), df_add(DyE, Dy0), C(cs.b13, q), df_add(DzE, Dz0));
+        dfl fW = shu(fE, 1);
+        if (tx == 0) {
+            const long long qw = q - 1;
+            const dfl DyW = D(qw + sj, qw - sj), DzW = D(qw + sk, qw - sk);
+            fW = df_dot3(C(cs.a1, qw), D(q, qw), C(cs.b12, qw), df_add(Dy0, DyW), C(cs.b13, qw), df_add(Dz0, DzW));
+        }
+        __syncthreads();
+        dfl DxN, DzN;
+        if (ty < 7 && j + 1 <= g.ny) {
+            DxN = sDx[buf][ty + 1][tx];
+            DzN = sDz[buf][ty + 1][tx];
+        } else {
+            const long long qn = q + sj;
+            DxN = D(qn + 1, qn - 1);
+            DzN = D(qn + sk, qn - sk);
+        }
+        const dfl fN = df_dot3(C(cs.a2, q), D(q + sj, q), C(cs.b21, q), df_add(DxN, Dx0), C(cs.b23, q), df_add(DzN, Dz0));
+        sN[buf][ty][tx] = fN;
+        __syncthreads();
+        dfl fS;
+        if (ty > 0) {
+            fS = sN[buf][ty - 1][tx];
+        } else {
+            const long long qs = q - sj;
+            const dfl DxS = D(qs + 1, qs - 1), DzS = D(qs + sk, qs - sk);
+            fS = df_dot3(C(cs.a2, qs), D(q, qs), C(cs.b21, qs), df_add(Dx0, DxS), C(cs.b23, qs), df_add(Dz0, DzS));
+        }
+        const dfl fF = df_dot3(C(cs.a3, q), D(qf, q), C(cs.b31, q), df_add(Dx1, Dx0), C(cs.b32, q), df_add(Dy1, Dy0));
+        if (act) {
+            const dfl r =
+                df_sub(df_from_double(b[q], ob), df_add(df_add(df_sub(fE, fW), df_sub(fN, fS)), df_sub(fF, fB)));
+            if constexpr (sizeof(Ti) == 4) {
+                rin[q] = df_to_float(r, ob);
+            } else {  // FP64 output (the residual entry point): head and tail unscaled exactly
+                rin[q] = ((double)r.h + (double)r.l) * (double)pow2f(-ob);
+            }
+            const float rf = __fadd_rn(r.h, r.l);
+            s = __fmaf_rn(rf, rf, s);
+            if (!tipo || tipo[q] == 2) m = fmaxf(m, fabsf(rf));  // max over fluid cells (tipo >= 2)
+        }
+        fB = fF;
+        Dx0 = Dx1;
+        Dy0 = Dy1;
+        Dz0 = Dz1;
+    }
+    const double un = (double)pow2f(-ob);
+    double sd = (double)s * un * un, md = (double)m * un;
+    block_reduce_sum_max(sd, md);
+    if (threadIdx.x == 0) {
+        const long long blk = ((long long)B.z * B.gy + B.y) * B.gx + B.x;
+        psq[blk] = sd;
+        pmax[blk] = md;
+    }
+}
+
+// split FP64 coefficients into double-floats times 2^oc
+__device__ __forceinline__ void k_split_coef_blk(long long n, Coef<double> c, Coef<float2> o, int oc, const Blk& B) {
+    const double* src[9] = {c.a1, c.b12, c.b13, c.a2, c.b21, c.b23, c.a3, c.b31, c.b32};
+    float2* dst[9] = {o.a1, o.b12, o.b13, o.a2, o.b21, o.b23, o.a3, o.b31, o.b32};
+    for (long long q = (long long)B.x * blockDim.x + threadIdx.x; q < n; q += (long long)B.gx * blockDim.x)
+#pragma unroll
+        for (int u = 0; u < 9; ++u) {
+            const dfl v = df_from_double(src[u][q], oc);
+            dst[u][q] = make_float2(v.h, v.l);
+        }
+}
+
+// the largest biased FP64 exponent of the nine coefficient boxes (atomicMax
+// into *out, cleared before)
+__device__ __forceinline__ void k_coef_exp_max_blk(long long n, Coef<double> c, int* out, const Blk& B) {
+    const double* src[9] = {c.a1, c.b12, c.b13, c.a2, c.b21, c.b23, c.a3, c.b31, c.b32};
+    int e = 0;
+    for (long long q = (long long)B.x * blockDim.x + threadIdx.x; q < n; q += (long long)B.gx * blockDim.x)
+#pragma unroll
+        for (int u = 0; u < 9; ++u) {
+            const int eb = (__double2hiint(src[u][q]) >> 20) & 0x7FF;
+            e = eb == 0x7FF ? e : max(e, eb);
+        }
+    e = __reduce_max_sync(0xffffffffu, e);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, e);
+}
+
 // the same residual when x is zero everywhere in the box: r = b exactly
 // (every flux vanishes), written and reduced with the same block layout
 template <typename Ti, int KC>

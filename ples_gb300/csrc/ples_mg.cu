@@ -63,6 +63,30 @@ __global__ void __launch_bounds__(256) k_resid_outer2(Geom g, Coef<double> c, co
     k_resid_outer2_blk<Ti, KC>(g, c, x, b, rin, psq, pmax, hw_blk(), tipo);
 }
 
+template <typename Ti, int KC>
+__global__ void __launch_bounds__(256, 4) k_resid_outer2_df(Geom g, Coef<float2> cs, const double* __restrict__ x,
+                                                         const double* __restrict__ b, Ti* __restrict__ rin,
+                                                         double* __restrict__ psq, double* __restrict__ pmax,
+                                                         const uint8_t* __restrict__ tipo, const int* __restrict__ sc) {
+    k_resid_outer2_df_blk<Ti, KC>(g, cs, x, b, rin, psq, pmax, hw_blk(), tipo, sc);
+}
+template <typename Ti, int KC>
+__global__ void __launch_bounds__(256, 4) k_resid_outer2_df_first(Geom g, Coef<float2> cs, const double* __restrict__ x,
+                                                               const double* __restrict__ b, Ti* __restrict__ rin,
+                                                               double* __restrict__ psq, double* __restrict__ pmax,
+                                                               const int* __restrict__ xnz,
+                                                               const uint8_t* __restrict__ tipo,
+                                                               const int* __restrict__ sc) {
+    if (*xnz == 0)
+        k_resid_zero_blk<Ti, KC>(g, b, rin, psq, pmax, hw_blk(), tipo);
+    else
+        k_resid_outer2_df_blk<Ti, KC>(g, cs, x, b, rin, psq, pmax, hw_blk(), tipo, sc);
+}
+__global__ void k_split_coef(long long n, Coef<double> c, Coef<float2> o, int oc) {
+    k_split_coef_blk(n, c, o, oc, hw_blk());
+}
+__global__ void k_coef_exp_max(long long n, Coef<double> c, int* out) { k_coef_exp_max_blk(n, c, out, hw_blk()); }
+
 // the first residual of a solve: the stencil is skipped when the initial
 // guess (wall ghosts included) is zero everywhere, *xnz == 0
 template <typename Ti, int KC>
@@ -784,6 +808,17 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     const double bnorm = bn2 > 0.0 ? std::sqrt(bn2) : 1.0;
     st->rhs_norm = std::sqrt(bn2);
     st->rhs_mean_removed = shift;
+    // mixed handles: the outer residual in double-float, scaled so that b's
+    // RMS lies in [1, 2) (ob) and the coefficients' largest in [1, 2) (oc)
+    const bool dfr = std::is_same<T, float>::value && F.has_cs;
+    if (dfr) {
+        const double rms = std::sqrt(bn2 / N);
+        const int ob = rms > 0.0 && std::isfinite(rms) ? std::min(100, std::max(-100, -(int)std::ilogb(rms))) : 0;
+        int* hs = reinterpret_cast<int*>(h->h_red + 6);
+        hs[0] = ob;
+        hs[1] = ob - h->oc;
+        CK(cudaMemcpyAsync(h->dscale, hs, 2 * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    }
 
     constexpr int kKC = 8;
     const dim3 rg((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kKC - 1) / kKC);
@@ -798,9 +833,16 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
             int* xnz = reinterpret_cast<int*>(h->red + 5);
             cudaMemsetAsync(xnz, 0, sizeof(int), h->st);
             k_box_nonzero<<<1216, 256, 0, h->st>>>(g.n, h->x, xnz);  // 8 CTAs per SM of a GB300
-            k_resid_outer2_first<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b,
-                                                               xnz, h->tipo);
+            if (dfr)
+                k_resid_outer2_df_first<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cs, h->x, h->b, (T*)F.rh, h->part_a,
+                                                                      h->part_b, xnz, h->tipo, h->dscale);
+            else
+                k_resid_outer2_first<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a,
+                                                                   h->part_b, xnz, h->tipo);
             ++h->launches;
+        } else if (dfr) {
+            k_resid_outer2_df<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cs, h->x, h->b, (T*)F.rh, h->part_a, h->part_b,
+                                                            h->tipo, h->dscale);
         } else {
             k_resid_outer2<T, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, h->x, h->b, (T*)F.rh, h->part_a, h->part_b,
                                                          h->tipo);
@@ -1418,6 +1460,21 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
             if (h->masked) mask_coef(h, n, L.cd);
             L.has_cd = true;
         }
+        if (n == 1 && mixed) {  // the double-float copy for the outer residual
+            int* ex;
+            if ((rc = dalloc(h, (void**)&ex, sizeof(int)))) { free_tmp(tmp); return rc; }
+            CK(cudaMemsetAsync(ex, 0, sizeof(int), h->st));
+            k_coef_exp_max<<<grid1(L.g.n), 256, 0, h->st>>>(L.g.n, L.cd, ex);
+            int emax = 0;
+            CK(cudaMemcpyAsync(&emax, ex, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
+            h->oc = emax > 0 ? std::min(100, std::max(-100, 1023 - emax)) : 0;
+            if ((rc = alloc_coef(h, L.g, L.cs))) { free_tmp(tmp); return rc; }
+            k_split_coef<<<grid1(L.g.n), 256, 0, h->st>>>(L.g.n, L.cd, L.cs, h->oc);
+            h->launches += 2;
+            CK(cudaGetLastError());
+            L.has_cs = true;
+        }
         if (mixed) {
             // the nine FP32 coefficient boxes, rh, c', 1/m and the two field
             // buffers of the level in one staggered allocation
@@ -1507,6 +1564,7 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
         (rc = dalloc(h, (void**)&h->part_b, 8 * (size_t)h->npart)) || (rc = dalloc(h, (void**)&h->red, 64)))
         return rc;
     h->dflag = reinterpret_cast<int*>(h->red + 4);
+    h->dscale = reinterpret_cast<int*>(h->red + 6);
     if ((rc = dalloc(h, (void**)&h->x2sync, sizeof(int) * ((size_t)g.nz + 3)))) return rc;
     CK(cudaMemsetAsync(h->x2sync, 0, sizeof(int) * ((size_t)g.nz + 3), h->st));
     CK(cudaMemsetAsync(h->red, 0, 64, h->st));
@@ -1791,11 +1849,59 @@ int ples_mg_get_metric(ples_mg_handle* h, int level, int which, double* out) {
     });
 }
 
+// the solve's own level-1 outer residual of (pr, rh), returned as L(pr) - rh:
+// the double-float kernel on a mixed handle (scaled as in the solve, by rh's
+// RMS), the FP64 one otherwise
+static int outer_residual(ples_mg_handle* h, const double* pr, const double* rh, double* out) {
+    LevelData& F = h->L[0];
+    const Geom& g = F.g;
+    std::vector<void*> tmp;
+    double *P, *R, *O;
+    int rc;
+    if ((rc = tmp_box(h, g, 8, (void**)&P, tmp)) || (rc = tmp_box(h, g, 8, (void**)&R, tmp)) ||
+        (rc = tmp_box(h, g, 8, (void**)&O, tmp)) || (rc = put_box(h, g, 1, pr, P, tmp)) ||
+        (rc = put_box(h, g, 0, rh, R, tmp))) {
+        free_tmp(tmp);
+        return rc;
+    }
+    constexpr int kKC = 8;
+    const dim3 rg((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kKC - 1) / kKC);
+    if (F.has_cs) {
+        const long long n = (long long)g.nx * g.ny * g.nz;
+        double s2 = 0.0;
+        for (long long q = 0; q < n; ++q) s2 += rh[q] * rh[q];
+        const double rms = std::sqrt(s2 / (double)n);
+        const int ob = rms > 0.0 && std::isfinite(rms) ? std::min(100, std::max(-100, -(int)std::ilogb(rms))) : 0;
+        int* hs = reinterpret_cast<int*>(h->h_red + 6);
+        hs[0] = ob;
+        hs[1] = ob - h->oc;
+        CK(cudaMemcpyAsync(h->dscale, hs, 2 * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        k_resid_outer2_df<double, kKC><<<rg, 256, 0, h->st>>>(g, F.cs, P, R, O, h->part_a, h->part_b, h->tipo,
+                                                              h->dscale);
+    } else {
+        k_resid_outer2<double, kKC><<<rg, 256, 0, h->st>>>(g, F.cd, P, R, O, h->part_a, h->part_b, h->tipo);
+    }
+    ++h->launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        free_tmp(tmp);
+        return fail(h, PLES_MG_CUDA_ERROR, "outer residual: %s", cudaGetErrorString(e));
+    }
+    rc = get_box(h, g, 0, O, out, tmp);
+    free_tmp(tmp);
+    if (rc) return rc;
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long q = 0; q < n; ++q) out[q] = -out[q];  // the kernels form rh - L(pr)
+    return PLES_MG_OK;
+}
+
 int ples_mg_apply_residual(ples_mg_handle* h, int level, const double* pr, const double* rh, double* out,
                            int precision) {
     if (!h || level < 1 || level > h->nlev || !pr || !rh || !out ||
-        (precision != PLES_MG_PREC_FP64 && precision != PLES_MG_PREC_MIXED))
+        (precision != PLES_MG_PREC_FP64 && precision != PLES_MG_PREC_MIXED && precision != PLES_MG_PREC_OUTER) ||
+        (precision == PLES_MG_PREC_OUTER && level != 1))
         return h ? fail(h, PLES_MG_BAD_ARG, "bad argument") : PLES_MG_BAD_ARG;
+    if (precision == PLES_MG_PREC_OUTER) return with_device(h, [&]() -> int { return outer_residual(h, pr, rh, out); });
     return with_device(h, [&]() -> int {
         std::vector<void*> tmp;
         const Geom& g = h->L[level - 1].g;

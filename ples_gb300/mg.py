@@ -21,7 +21,7 @@ import numpy as np
 from . import build as _build
 
 OK, NOT_CONVERGED, BAD_ARG, OOM, DEVICE_TIMEOUT, CUDA_ERROR, DIVERGED, NO_DEVICE = range(8)
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_OUTER = 0, 1, 2
 COORDS_NODES, COORDS_GHOSTED8 = 0, 1
 METRIC_NAMES = ("g11", "g12", "g13", "g21", "g22", "g23", "g31", "g32", "g33")
 
@@ -405,9 +405,12 @@ class Multigrid:
         return out
 
     def residual(self, level, pr, rh, precision="fp64"):
+        """L(pr) - rh at one level (ples_mg_apply_residual): the FP64 kernel,
+        the FP32 one ("fp32"), or ("outer", level 1) the one the solve's stop
+        test uses: double-float products on a mixed handle."""
         nx, ny, nz = self.dims(level)
         out = np.zeros((nx, ny, nz), order="F")
-        p = {"fp64": PREC_FP64, "fp32": PREC_MIXED, "mixed": PREC_MIXED}[precision]
+        p = {"fp64": PREC_FP64, "fp32": PREC_MIXED, "mixed": PREC_MIXED, "outer": PREC_OUTER}[precision]
         self._check(self._L.ples_mg_apply_residual(self._h, level, _f64(pr), _f64(rh), out, p))
         return out
 
