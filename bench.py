@@ -636,7 +636,7 @@ def _report(args, m, w, ws, rank, dist, value, ms_per_step, outer, relres, t64, 
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded wavy-wall channel grid and divergence RHS)",
         "config": _workload_config(w),
-        "solver": {"precision": "mixed: FP32 V-cycle, FP64 residual/update/projection",
+        "solver": {"precision": "mixed: FP32 V-cycle; FP64 update/projection; outer residual FP64 differences, double-float products",
                    "parallelism": f"replicas x{ws}", "levels": m.nlevel,
                    "outer_iterations_mean": outer, "max_rel_residual": relres},
         "fp64": {"value": 1.0 / t64 if t64 else None, "unit": UNIT,
