@@ -56,15 +56,21 @@ typedef struct {
                               jp must be 1 (multigrid.f03:1744-1746)                */
     int nlevmax;           /* maximum multigrid levels; 0 = automatic: coarsen until a level has
                               at most 3072 unknowns (wall rows included), solved by a dense inverse */
-    double omega;          /* relaxation factor of the line smoother (0 = default)   */
+    double omega;          /* relaxation factor of the smoother (0 = default: 1.4 for
+                              smoothers 0 and 2, 0.8 for 1, 1.0 for 3)          */
     int precision;         /* PLES_MG_PREC_*                                        */
     int coords_layout;     /* PLES_MG_COORDS_*                                      */
     const double *x, *y, *z; /* host node coordinates, column-major                 */
     double dt;             /* time step dividing the cs1..cs6 wall fluxes           */
     int device;            /* CUDA device ordinal                                   */
-    int nu_pre, nu_post;   /* smoothing sweeps per level (0 = default)              */
+    int nu_pre, nu_post;   /* smoothing sweeps per level before / after the coarse
+                              correction (0 = default: 1 / 2 for smoothers 0 and 2
+                              with an even inner_cycles, else 2 / 2); the sweeps of
+                              one outer iteration, (nu_pre + nu_post) x
+                              inner_cycles, must be even                        */
     int nu_coarse;         /* sweeps on the coarsest level (0 = default)            */
-    int inner_cycles;      /* V-cycles per outer FP64 iteration (0 = default)       */
+    int inner_cycles;      /* V-cycles per outer FP64 iteration (0 = default: 6 for
+                              smoothers 0 and 2, else 5)                        */
     int smoother;          /* 0 = zebra eta-line SOR (Gauss-Seidel in x and z as the
                               reference's line SOR, islor = 1); 1 = eta-line Jacobi;
                               2 = zebra with its rows staged by TMA (FP32);
@@ -260,17 +266,20 @@ int ples_mg_read_grid(const char *path, double lengths[3], int dims[3], double *
  * inputs).  Times candidate settings on this handle's grid and keeps the
  * fastest: the form of the eta-line smoother per level (128, 256 or 512
  * threads on 32-line tiles, or 1024 for 512 threads on 64-line tiles, by
- * kernel time) and then the sweeps per level (nu_pre = nu_post
- * in 1..3) and V-cycles per outer iteration (2 to 6), by the time of a
- * whole solve to ||r||/||b|| <= 1e-10 from zero.  rhs (host, (1:jx,1:jy,
+ * kernel time) and then the sweeps per level before and after the coarse
+ * correction (1..3 each, seven pairs), the V-cycles per outer iteration (2
+ * to 8) and, for the zebra smoothers, omega (the handle's, 1.3, 1.4), by
+ * the time of a whole solve to ||r||/||b|| <= 1e-10 from zero.  rhs (host, (1:jx,1:jy,
  * 1:jz)) or NULL for a pseudo-random compatible one.  Batches created
  * afterwards use the tuned settings of their members. */
 typedef struct {
-    int nu;               /* sweeps per level before and after the coarse correction */
+    int nu;               /* sweeps per level before the coarse correction (nu_pre) */
     int inner_cycles;     /* V-cycles per FP64 outer iteration */
     int line_threads[12]; /* smoother form per level, as ples_mg_set_line_threads (0 past the last level) */
     double solve_ms;      /* one solve with the chosen setting */
     int candidates;       /* settings timed */
+    int nu_post;          /* sweeps per level after the coarse correction */
+    double omega;         /* relaxation factor */
 } ples_mg_tuning;
 int ples_mg_autotune(ples_mg_handle *h, const double *rhs, ples_mg_tuning *out);
 /* Set the form of the eta-line smoother at one level (1-based), as the
@@ -300,7 +309,7 @@ int ples_mg_get_line_threads(const ples_mg_handle *h, int level, int *threads);
 /* ---- many grids at once ------------------------------------------------
  * No counterpart in the reference, which solves one grid per run.  A batch
  * groups existing handles (mixed precision, zebra smoother, full
- * coarsening, nu_pre == nu_post, periodic x and z, a dense coarsest level,
+ * coarsening, periodic x and z, a dense coarsest level,
  * all on one device; immersed-boundary masks and cell types allowed); each
  * keeps its resident hierarchy.  One outer iteration of all members is a captured
  * CUDA graph of persistent step kernels that walk (member, level, tile)

@@ -365,12 +365,13 @@ int build_steps(ples_mg_batch* b) {
     const bool allow_wide = b->smem_wide <= 227 * 1024;
     // buffer roles per member and level: 0 -> (p, p2), 1 -> (p2, p)
     std::vector<std::vector<int>> cur(nm);
-    int lmax = 0, numax = 0, inmax = 0, wmax = 0;
+    int lmax = 0, numax = 0, nupmax = 0, inmax = 0, wmax = 0;
     for (int i = 0; i < nm; ++i) {
         ples_mg_handle* h = b->mem[i];
         cur[i].assign(h->nlev, 0);
         lmax = std::max(lmax, h->nlev);
         numax = std::max(numax, h->nu_pre);
+        nupmax = std::max(nupmax, h->nu_post);
         inmax = std::max(inmax, h->inner_cycles);
         wmax = std::max(wmax, h->wall_passes);
     }
@@ -444,13 +445,15 @@ int build_steps(ples_mg_batch* b) {
         }
         B.end();
     };
-    auto line_steps = [&](int c, int n, int s, bool zin) {  // one sweep of level n for the members in it
+    // one sweep of level n for the members in it (s: the sweep's index among
+    // the pre-smoothing sweeps, or the post-smoothing ones when post)
+    auto line_steps = [&](int c, int n, int s, bool zin, bool post) {
         for (int par = 0; par < 2; ++par) {
             B.begin<LineTask>(zin ? K_LINE1 : K_LINE0, PH_ITER);
             long long big = -1;
             for (int i = 0; i < nm; ++i) {
                 ples_mg_handle* h = b->mem[i];
-                if (c >= h->inner_cycles || n > h->nlev - 2 || s >= h->nu_pre) continue;
+                if (c >= h->inner_cycles || n > h->nlev - 2 || s >= (post ? h->nu_post : h->nu_pre)) continue;
                 const LevelData& L = h->L[n];
                 LineTask t{};
                 t.h.inst = i;
@@ -478,7 +481,7 @@ int build_steps(ples_mg_batch* b) {
         }
         for (int i = 0; i < nm; ++i) {
             ples_mg_handle* h = b->mem[i];
-            if (c >= h->inner_cycles || n > h->nlev - 2 || s >= h->nu_pre) continue;
+            if (c >= h->inner_cycles || n > h->nlev - 2 || s >= (post ? h->nu_post : h->nu_pre)) continue;
             cur[i][n] ^= 1;
         }
     };
@@ -551,7 +554,7 @@ int build_steps(ples_mg_batch* b) {
     red_step(PH_ITER, RED_DECIDE, 1);
     for (int c = 0; c < inmax; ++c) {
         for (int n = 0; n + 1 < lmax; ++n) {
-            for (int s = 0; s < numax; ++s) line_steps(c, n, s, s == 0 && (n > 0 || c == 0));
+            for (int s = 0; s < numax; ++s) line_steps(c, n, s, s == 0 && (n > 0 || c == 0), false);
             B.begin<RRTask>(K_RR, PH_ITER);
             for (int i = 0; i < nm; ++i) {
                 ples_mg_handle* h = b->mem[i];
@@ -606,7 +609,7 @@ int build_steps(ples_mg_batch* b) {
                 B.add(t, prol_grid(F.g, C.g));
             }
             B.end();
-            for (int s = 0; s < numax; ++s) line_steps(c, n, s, false);
+            for (int s = 0; s < nupmax; ++s) line_steps(c, n, s, false, true);
         }
     }
     B.begin<UpdTask>(K_UPD, PH_ITER);
@@ -708,8 +711,6 @@ int batch_create(ples_mg_handle* const* members, int n, ples_mg_batch* b) {
                          "member %d: batched solves need mixed precision, the zebra smoother and full coarsening", i);
         if (!h->coarse_S) return bfail(b, PLES_MG_BAD_ARG, "member %d: coarsest level too large for the dense solve", i);
         if (h->walls_xz) return bfail(b, PLES_MG_BAD_ARG, "member %d: x or z walls are not batched", i);
-        if (h->nu_pre != h->nu_post)
-            return bfail(b, PLES_MG_BAD_ARG, "member %d: batched solves need nu_pre == nu_post", i);
         for (int l = 1; l < h->nlev; ++l)
             if (h->L[l].rx != 2) return bfail(b, PLES_MG_BAD_ARG, "member %d: level %d not coarsened in x", i, l + 1);
         if (h->dev != members[0]->dev) return bfail(b, PLES_MG_BAD_ARG, "members live on different devices");

@@ -757,6 +757,14 @@ struct NvtxSpan {  // a range opened and closed at run time, closed at scope exi
     ~NvtxSpan() { end(); }
 };
 
+// the relaxation factor's bits, a key of the captured solve graphs (the
+// smoother launches carry omega as an argument)
+long long omega_bits(double om) {
+    long long b;
+    std::memcpy(&b, &om, sizeof b);
+    return b;
+}
+
 template <typename T>
 int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles, ples_mg_stats* st) {
     NvtxRange range("ples_mg solve");
@@ -864,7 +872,7 @@ int solve_core(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles
     if (graphs) {
         std::vector<long long> key = {(long long)sizeof(T), h->inner_cycles, h->nu_pre, h->nu_post, h->nu_coarse,
                                       h->timed_kind, h->timed_level,
-                                      h->smoother, h->wall_passes, (long long)h->wait_polls,
+                                      h->smoother, h->wall_passes, (long long)h->wait_polls, omega_bits(h->omega),
                                       (long long)(uintptr_t)h->cs_c[0],
                                       (long long)(uintptr_t)h->cs_c[1], (long long)(uintptr_t)h->cs_c[2],
                                       (long long)(uintptr_t)h->cs_c[3], (long long)(uintptr_t)h->cs_c[4],
@@ -1353,14 +1361,22 @@ int create_impl(const ples_mg_desc* d, ples_mg_handle* h) {
     CK(cudaSetDevice(h->dev));
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     h->smoother = d->smoother;
-    h->omega = d->omega > 0.0 ? d->omega : (d->smoother == 1 ? 0.8 : (d->smoother == 3 ? 1.0 : 1.3));
+    // defaults measured on GB300 (whole solves to 1e-10 on channels from
+    // 96x48x96 to 256x128x256): for the zebra smoothers one sweep before and
+    // two after the coarse correction, six V-cycles per outer iteration and
+    // omega 1.4 (20.4 ms against 21.6 with 2 / 2, 5 and 1.3 on 256x128x256;
+    // 13.8 against 18.1 on 192x96x192)
+    const bool zebra = d->smoother == 0 || d->smoother == 2;
+    h->omega = d->omega > 0.0 ? d->omega : (d->smoother == 1 ? 0.8 : (d->smoother == 3 ? 1.0 : 1.4));
     h->fs = d->freesurface != 0;
-    h->nu_pre = d->nu_pre ? d->nu_pre : 2;
-    h->nu_post = d->nu_post ? d->nu_post : 2;
+    h->inner_cycles = d->inner_cycles ? d->inner_cycles : (zebra ? 6 : 5);
+    const bool asym = zebra && h->inner_cycles % 2 == 0;  // 1 + 2 sweeps: an even count per outer iteration
+    h->nu_pre = d->nu_pre ? d->nu_pre : (asym ? 1 : 2);
+    h->nu_post = d->nu_post ? d->nu_post : (asym ? 2 : 2);
     // sweeps on a smoothed coarsest level (x / z walls, no dense inverse): 10,
     // the reference's coarse-level kss; otherwise the coarsest is dense
     h->nu_coarse = d->nu_coarse ? d->nu_coarse : ((d->ip || d->kp) ? 10 : 40);
-    h->inner_cycles = d->inner_cycles ? d->inner_cycles : 5;
+
     const int jx = d->jx, jy = d->jy, jz = d->jz;
     // nodes (host copy needed for the spacings)
     const size_t nn = (size_t)(jx + 1) * (jy + 1) * (jz + 1);
@@ -2496,24 +2512,44 @@ int ples_mg_autotune(ples_mg_handle* h, const double* rhs, ples_mg_tuning* out) 
             h->L[n].line_threads = bt;
         }
         ples_mg_kernel_timing(h, -1, 0);
-        int bnu = h->nu_pre, bin = h->inner_cycles;
-        double bms = 1e300;
-        for (int nu : {1, 2, 3})
-            for (int inner : {2, 3, 4, 5, 6}) {
-                h->nu_pre = h->nu_post = nu;
-                h->inner_cycles = inner;
-                if ((rc = trial(1, &ms, &st)) || (rc = trial(2, &ms, &st))) return rc;
-                ++tried;
-                if (st.status == PLES_MG_OK && ms < bms) {
-                    bms = ms;
-                    bnu = nu;
-                    bin = inner;
+        // then the sweeps before / after the coarse correction, the V-cycles
+        // per outer iteration and (zebra smoothers) omega; a setting whose
+        // sweeps per outer iteration are odd is not a candidate
+        int bpre = h->nu_pre, bpost = h->nu_post, bin = h->inner_cycles;
+        double bom = h->omega, bms = 1e300;
+        const bool zebra = h->smoother == 0 || h->smoother == 2;
+        std::vector<double> oms = {h->omega};
+        if (zebra) {
+            for (double o : {1.3, 1.4})
+                if (o != h->omega) oms.push_back(o);
+        }
+        const int pairs[7][2] = {{1, 1}, {1, 2}, {2, 1}, {2, 2}, {1, 3}, {2, 3}, {3, 3}};
+        for (double om : oms)
+            for (const auto& pp : pairs)
+                for (int inner : {2, 3, 4, 5, 6, 8}) {
+                    if ((pp[0] + pp[1]) * inner % 2) continue;
+                    h->omega = om;
+                    h->nu_pre = pp[0];
+                    h->nu_post = pp[1];
+                    h->inner_cycles = inner;
+                    if ((rc = trial(1, &ms, &st)) || (rc = trial(2, &ms, &st))) return rc;
+                    ++tried;
+                    if (st.status == PLES_MG_OK && ms < bms) {
+                        bms = ms;
+                        bpre = pp[0];
+                        bpost = pp[1];
+                        bin = inner;
+                        bom = om;
+                    }
                 }
-            }
-        h->nu_pre = h->nu_post = bnu;
+        h->omega = bom;
+        h->nu_pre = bpre;
+        h->nu_post = bpost;
         h->inner_cycles = bin;
         std::memset(out, 0, sizeof *out);
-        out->nu = bnu;
+        out->nu = bpre;
+        out->nu_post = bpost;
+        out->omega = bom;
         out->inner_cycles = bin;
         for (int n = 0; n < h->nlev && n < 12; ++n) out->line_threads[n] = h->L[n].line_threads;
         out->solve_ms = bms;

@@ -46,7 +46,7 @@ class Desc(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("nu", C.c_int), ("inner_cycles", C.c_int), ("line_threads", C.c_int * 12),
-                ("solve_ms", C.c_double), ("candidates", C.c_int)]
+                ("solve_ms", C.c_double), ("candidates", C.c_int), ("nu_post", C.c_int), ("omega", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -340,13 +340,14 @@ class Multigrid:
         return arrs, st.as_dict()
 
     def autotune(self, rhs=None):
-        """Time candidate smoother widths, sweep counts and inner cycles on
-        this grid and keep the fastest (ples_mg_autotune)."""
+        """Time candidate smoother widths, sweep counts (before / after the
+        coarse correction), inner cycles and omega on this grid and keep the
+        fastest (ples_mg_autotune)."""
         t = Tuning()
         keep = None if rhs is None else _f64(rhs)
         ptr = None if keep is None else C.c_void_p(keep.ctypes.data)
         self._check(self._L.ples_mg_autotune(self._h, ptr, C.byref(t)))
-        return {"nu": t.nu, "inner_cycles": t.inner_cycles,
+        return {"nu": t.nu, "nu_pre": t.nu, "nu_post": t.nu_post, "omega": t.omega, "inner_cycles": t.inner_cycles,
                 "line_threads": [v for v in t.line_threads if v], "solve_ms": t.solve_ms,
                 "candidates": t.candidates}
 

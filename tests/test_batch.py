@@ -172,7 +172,8 @@ def test_autotune_then_batch(cases):
     members = [mg.Multigrid(*c[:3]) for c in sub]
     tuned = [m.autotune(c[3]) for m, c in zip(members, sub)]
     for t in tuned:
-        assert t["nu"] in (1, 2, 3) and t["inner_cycles"] in (2, 3, 4, 5, 6)
+        assert t["nu_pre"] in (1, 2, 3) and t["nu_post"] in (1, 2, 3) and t["inner_cycles"] in (2, 3, 4, 5, 6, 8)
+        assert (t["nu_pre"] + t["nu_post"]) * t["inner_cycles"] % 2 == 0 and t["omega"] in (1.3, 1.4)
         assert set(t["line_threads"]) <= {128, 256, 512, 1024} and t["candidates"] >= 13
     with mg.Batch(members) as b:
         fis, sts = b.solve([c[3] for c in sub], rel_tol=REL_TOL)

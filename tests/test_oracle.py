@@ -217,6 +217,25 @@ def test_point_sor_diverges_on_stretched_channel_but_line_sor_converges():
     assert rr_slor <= 1e-10 and cyc < 30
 
 
+def test_line_sor_diverges_with_x_walls_on_wavy_stretched_channel():
+    """With walls in x (ip = 1) on a wavy (A = 0.1), strongly stretched
+    (beta = 2.5) channel the reference's own line-SOR multigrid ends in NaN,
+    as it does with walls in x and z; the same grid with z walls only, or
+    with milder stretching, converges.  The device solver reports this case
+    as diverged (tests/test_walls.py)."""
+    dims = (64, 32, 64)
+    x, y, z = S.wavy_channel_grid(*dims, 0.1, 2.5)
+    rhs = S.divergence_rhs(*dims, seed=4)
+    for ip, kp, npr in ((1, 0, 1), (1, 1, 2)):
+        _, _, _, rr = Oracle(x, y, z, ip=ip, kp=kp, islor=1, nproc=npr).multi(rhs, eps=1e-10, ficycle=200)
+        assert not np.isfinite(rr), (ip, kp, rr)
+    _, _, _, rr = Oracle(x, y, z, ip=0, kp=1, islor=1, nproc=2).multi(rhs, eps=1e-10, ficycle=200)
+    assert rr <= 1e-10
+    x, y, z = S.wavy_channel_grid(*dims, 0.1, 1.0)
+    _, _, _, rr = Oracle(x, y, z, ip=1, kp=0, islor=1).multi(rhs, eps=1e-10, ficycle=200)
+    assert rr <= 1e-10
+
+
 def test_bad_arguments_rejected():
     x, y, z = S.wavy_channel_grid(32, 16, 32, 0.05, 2.0)
     with pytest.raises(ValueError):

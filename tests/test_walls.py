@@ -202,3 +202,17 @@ def test_steep_wall_grid_never_returns_garbage():
             assert np.linalg.norm(r) / np.linalg.norm(rhs) <= 1e-8
         fi, st = m.solve(np.zeros((32, 16, 32), order="F"), rel_tol=1e-10)
         assert st["status"] == mg.OK
+
+
+def test_divergent_wall_case_is_reported():
+    """x and z walls on a wavy, strongly stretched channel: the reference's
+    iteration itself ends in NaN there (tests/test_oracle.py); the device
+    solve stops with PLES_MG_DIVERGED rather than returning a field."""
+    from ples_gb300 import mg
+    dims = (64, 32, 64)
+    x, y, z = S.wavy_channel_grid(*dims, 0.1, 2.5)
+    rhs = S.divergence_rhs(*dims, seed=4)
+    with mg.Multigrid(x, y, z, ip=1, kp=1) as m:
+        with pytest.raises(mg.PlesMGError) as e:
+            m.solve(rhs, rel_tol=1e-10, max_cycles=40)
+    assert e.value.code == mg.DIVERGED
