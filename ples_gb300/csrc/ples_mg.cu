@@ -1025,106 +1025,89 @@ double mean_spacing(const double* x, const double* y, const double* z, int jx, i
 }
 
 // Gauss-Jordan inversion with partial pivoting on the device (FP64), one
-// pivot column per step.  K (m x m) is reduced to the identity while the
-// same row operations build its inverse E.  E is kept with its columns in
-// pivot order, S(:,c) = E(:,perm(c)) for the original row perm(c) chosen at
-// step c: before its step a column of E is a unit vector that need not be
-// stored, so step col works on the K columns after col and the S columns up
-// to col only, m per row in all.
-//   k_gj_pivot      one CTA: the row p >= col of largest |K(p,col)|; keeps
-//                   K(p,col) and K(col,col) for the step
-//   k_gj_swap_scale thread t: rows p and col swapped in K column t >= col
-//                   and S column t < col, the pivot row scaled by
-//                   1/K(p,col); the elimination factors f(r) = K(r,col)
-//                   after the swap (0 for the pivot row); perm updated
-//   k_gj_eliminate  one CTA per row r with f(r) != 0: K(r,q) -= f(r) K(col,q)
-//                   for q > col, S(r,c) -= f(r) S(col,c) for c < col, and
-//                   the new column S(r,col) = -f(r) / K(p,col)
-struct GjStep {
-    int piv;
-    int bad;
-    double pv, kcc;
-};
-__global__ void k_gj_pivot(const double* __restrict__ K, int m, int col, GjStep* st) {
-    __shared__ double bv[1024];
-    __shared__ int bi[1024];
-    double best = -1.0;
-    int arg = col;
-    for (int r = col + (int)threadIdx.x; r < m; r += blockDim.x) {
-        const double v = fabs(K[(size_t)r * m + col]);
-        if (v > best) { best = v; arg = r; }
+// launch per pivot column.  K (m x m) is reduced to a row-permuted diagonal
+// while the same row operations build E; the pivot rows stay where they are
+// and unscaled (row p_c keeps its pivot K(p_c, c), and the inverse's row c
+// is E's row p_c divided by it at the end).  So a step reads the pivot row,
+// which no CTA writes during it, and every CTA writes only its own row.  E
+// is kept with its columns in pivot order, S(:, c) = E(:, p_c): before step
+// c that column is the unit vector of row p_c, so step c works on the K
+// columns after c and the S columns up to c only, m per row in all.
+//   k_gj_first  the pivot key of column 0
+//   k_gj_step   one CTA per row r: p = the pivot of column c (from its key);
+//               row p records itself (S(p, c) = 1, used, pivrow[c] = p); any
+//               other row with f = K(r, c) / K(p, c) != 0 takes
+//               K(r, q) -= f K(p, q) for q > c, S(r, j) -= f S(p, j) for
+//               j < c and S(r, c) = -f; then every unused row offers
+//               |K(r, c + 1)| for the next pivot
+// A pivot key packs the high word of |v| (sign, exponent and 20 significand
+// bits) over m - r into 64 bits, so atomicMax picks the largest magnitude
+// to 20 bits, ties to the lowest row; key 0 (no candidate left) marks the
+// system singular.  Each column has kGjSlots keys, row r offering to slot
+// r mod kGjSlots (one address taking every row's atomic serialises the
+// step); the step that uses a column reduces its slots with one warp.
+constexpr int kGjSlots = 32;
+__device__ __forceinline__ void gj_offer(unsigned long long* key, double v, int r, int m) {
+    if (v > 0.0)
+        atomicMax(key + r % kGjSlots,
+                  ((unsigned long long)(unsigned)__double2hiint(v) << 32) | (unsigned long long)(unsigned)(m - r));
+}
+__global__ void k_gj_first(const double* __restrict__ K, int m, unsigned long long* __restrict__ keys) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < m) gj_offer(keys, fabs(K[(size_t)r * m]), r, m);
+}
+__global__ void k_gj_step(double* __restrict__ K, double* __restrict__ S, int m, int c,
+                          unsigned long long* __restrict__ keys, int* __restrict__ used, int* __restrict__ pivrow,
+                          int* __restrict__ bad) {
+    __shared__ unsigned long long s_key;
+    if (threadIdx.x < 32) {  // the column's key: the largest of its slots
+        unsigned long long k = keys[(size_t)c * kGjSlots + threadIdx.x];
+        for (int o = 16; o; o >>= 1) {
+            const unsigned long long t = __shfl_xor_sync(0xffffffffu, k, o);
+            k = t > k ? t : k;
+        }
+        if (threadIdx.x == 0) s_key = k;
     }
-    bv[threadIdx.x] = best;
-    bi[threadIdx.x] = arg;
     __syncthreads();
-    for (int o = blockDim.x / 2; o; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            const double v = bv[threadIdx.x + o];
-            const int a = bi[threadIdx.x + o];
-            if (v > bv[threadIdx.x] || (v == bv[threadIdx.x] && a < bi[threadIdx.x])) {
-                bv[threadIdx.x] = v;
-                bi[threadIdx.x] = a;
-            }
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const int p = bi[0];
-        st->piv = p;
-        if (!(bv[0] > 0.0)) st->bad = 1;
-        st->pv = K[(size_t)p * m + col];
-        st->kcc = K[(size_t)col * m + col];
-    }
-}
-__global__ void k_gj_swap_scale(double* __restrict__ K, double* __restrict__ S, double* __restrict__ f,
-                                int* __restrict__ perm, int m, int col, const GjStep* st) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m || st->bad) return;
-    const int p = st->piv;
-    const double inv = 1.0 / st->pv;
-    // factor of row t after the swap (rows other than p and col keep theirs)
-    f[t] = t == col ? 0.0 : (t == p ? st->kcc : K[(size_t)t * m + col]);
-    if (t >= col) {
-        const double ka = K[(size_t)p * m + t], kb = K[(size_t)col * m + t];
-        if (p != col) K[(size_t)p * m + t] = kb;
-        K[(size_t)col * m + t] = ka * inv;
-    }
-    if (t < col) {
-        const double sa = S[(size_t)p * m + t], sb = S[(size_t)col * m + t];
-        if (p != col) S[(size_t)p * m + t] = sb;
-        S[(size_t)col * m + t] = sa * inv;
-    } else if (t == col) {
-        S[(size_t)col * m + col] = inv;  // the unit column of the pivot row, scaled
-        if (p != col) {
-            const int o = perm[p];
-            perm[p] = perm[col];
-            perm[col] = o;
-        }
-    }
-}
-__global__ void k_gj_eliminate(double* __restrict__ K, double* __restrict__ S, const double* __restrict__ f, int m,
-                               int col, const GjStep* st) {
+    const unsigned long long key = s_key;
     const int r = blockIdx.x;
-    if (r == col || st->bad) return;
-    const double fr = f[r];
-    if (fr == 0.0) return;
+    if (key == 0ull) {
+        if (r == 0 && threadIdx.x == 0) *bad = 1;
+        return;
+    }
+    const int p = m - (int)(unsigned)(key & 0xffffffffull);
     double* Kr = K + (size_t)r * m;
-    const double* Kc = K + (size_t)col * m;
-    for (int q = col + 1 + (int)threadIdx.x; q < m; q += blockDim.x) Kr[q] -= fr * Kc[q];
     double* Sr = S + (size_t)r * m;
-    const double* Sc = S + (size_t)col * m;
-    for (int c = threadIdx.x; c < col; c += blockDim.x) Sr[c] -= fr * Sc[c];
-    if (threadIdx.x == 0) Sr[col] = -fr / st->pv;
+    if (r == p) {
+        if (threadIdx.x == 0) {
+            Sr[c] = 1.0;
+            used[r] = 1;
+            pivrow[c] = r;
+        }
+        return;
+    }
+    const double* Kp = K + (size_t)p * m;
+    const double* Sp = S + (size_t)p * m;
+    const double f = Kr[c] / Kp[c];
+    if (f != 0.0) {
+        for (int q = c + 1 + (int)threadIdx.x; q < m; q += blockDim.x) Kr[q] -= f * Kp[q];
+        for (int j = threadIdx.x; j < c; j += blockDim.x) Sr[j] -= f * Sp[j];
+        if (threadIdx.x == 0) Sr[c] = -f;
+    }
+    // thread 0 updated K(r, c + 1) itself (the first q of its loop)
+    if (threadIdx.x == 0 && c + 1 < m && !used[r]) gj_offer(keys + (size_t)(c + 1) * kGjSlots, fabs(Kr[c + 1]), r, m);
 }
-// the inverse of the bordered system without its border: Inv(r, perm(c)) = S(r, c)
+// the inverse of the bordered system without its border: row c of the
+// inverse is row pivrow[c] of S over its pivot, column j of S is unknown
+// pivrow[j]
 template <typename T>
-__global__ void k_gj_extract(const double* __restrict__ S, const int* __restrict__ perm, int m, int n,
-                             T* __restrict__ out) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r = blockIdx.y;
-    if (c >= m) return;
-    const int o = perm[c];
-    if (o < n) out[(size_t)r * n + o] = T(S[(size_t)r * m + c]);
+__global__ void k_gj_extract(const double* __restrict__ K, const double* __restrict__ S,
+                             const int* __restrict__ pivrow, int m, int n, T* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (j >= m || c >= n) return;
+    const int r = pivrow[c], o = pivrow[j];
+    if (o < n) out[(size_t)c * n + o] = T(S[(size_t)r * m + j] / K[(size_t)r * m + c]);
 }
 
 // dense inverse of the bordered coarsest system [[M, v], [1^T, 0]] (M: the
@@ -1232,8 +1215,6 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         K[(size_t)n * m + n] = 1.0;
     }
     // Gauss-Jordan inverse with partial pivoting, on the device
-    std::vector<int> perm0(m);
-    for (int u = 0; u < m; ++u) perm0[u] = u;
     std::vector<void*> tmp;
     auto talloc = [&](void** p, size_t bytes) -> int {
         if (cudaMalloc(p, bytes) != cudaSuccess) {
@@ -1244,33 +1225,30 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         tmp.push_back(*p);
         return PLES_MG_OK;
     };
-    double *dK, *dI, *dF;
-    int* dP;
-    GjStep* dS;
+    double *dK, *dI;
+    unsigned long long* dKey;
+    int *dUsed, *dPiv, *dBad;
     int rc;
     if ((rc = talloc((void**)&dK, 8 * (size_t)m * m)) || (rc = talloc((void**)&dI, 8 * (size_t)m * m)) ||
-        (rc = talloc((void**)&dF, 8 * (size_t)m)) || (rc = talloc((void**)&dP, sizeof(int) * (size_t)m)) ||
-        (rc = talloc((void**)&dS, sizeof(GjStep))))
+        (rc = talloc((void**)&dKey, 8 * ((size_t)m + 1) * kGjSlots)) || (rc = talloc((void**)&dUsed, sizeof(int) * (size_t)m)) ||
+        (rc = talloc((void**)&dPiv, sizeof(int) * (size_t)m)) || (rc = talloc((void**)&dBad, sizeof(int))))
         return rc;
     auto gj = [&]() -> int {
         CK(cudaMemcpyAsync(dK, K.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemsetAsync(dI, 0, 8 * (size_t)m * m, h->st));
-        CK(cudaMemcpyAsync(dP, perm0.data(), sizeof(int) * (size_t)m, cudaMemcpyHostToDevice, h->st));
-        CK(cudaMemsetAsync(dS, 0, sizeof(GjStep), h->st));
-        const int tb = 256, nb = (m + tb - 1) / tb;
-        for (int col = 0; col < m; ++col) {
-            k_gj_pivot<<<1, 1024, 0, h->st>>>(dK, m, col, dS);
-            k_gj_swap_scale<<<nb, tb, 0, h->st>>>(dK, dI, dF, dP, m, col, dS);
-            k_gj_eliminate<<<m, tb, 0, h->st>>>(dK, dI, dF, m, col, dS);
-        }
-        h->launches += 3LL * m;
+        CK(cudaMemsetAsync(dKey, 0, 8 * ((size_t)m + 1) * kGjSlots, h->st));
+        CK(cudaMemsetAsync(dUsed, 0, sizeof(int) * (size_t)m, h->st));
+        CK(cudaMemsetAsync(dBad, 0, sizeof(int), h->st));
+        k_gj_first<<<(m + 255) / 256, 256, 0, h->st>>>(dK, m, dKey);
+        for (int col = 0; col < m; ++col) k_gj_step<<<m, 256, 0, h->st>>>(dK, dI, m, col, dKey, dUsed, dPiv, dBad);
+        h->launches += 1LL + m;
         CK(cudaGetLastError());
-        GjStep hs;
-        CK(cudaMemcpyAsync(&hs, dS, sizeof(GjStep), cudaMemcpyDeviceToHost, h->st));
+        int hbad = 0;
+        CK(cudaMemcpyAsync(&hbad, dBad, sizeof(int), cudaMemcpyDeviceToHost, h->st));
         CK(cudaStreamSynchronize(h->st));
-        if (hs.bad) return fail(h, PLES_MG_BAD_ARG, "coarsest-level system is singular");
+        if (hbad) return fail(h, PLES_MG_BAD_ARG, "coarsest-level system is singular");
         if ((rc = dalloc(h, &h->coarse_S, sizeof(T) * (size_t)n * n))) return rc;
-        k_gj_extract<T><<<dim3((m + 255) / 256, n), 256, 0, h->st>>>(dI, dP, m, n, (T*)h->coarse_S);
+        k_gj_extract<T><<<dim3((m + 255) / 256, n), 256, 0, h->st>>>(dK, dI, dPiv, m, n, (T*)h->coarse_S);
         ++h->launches;
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(h->st));
