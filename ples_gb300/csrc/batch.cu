@@ -78,7 +78,7 @@ struct RoutTask { TaskHead h; Geom g; Coef<double> c; const double* x; const dou
 struct LineTask { TaskHead h; Geom g; Coef<float> c; const float* cp; const float* pin; const float* pk; float* pout; const float* rh; float omega; int kpar; int zk; int wide; };
 struct RRTask { TaskHead h; Geom gf, gc; Coef<float> c; const float* p; const float* rh; float* rhc; int rx, ry, rz; };
 struct DenseTask { TaskHead h; Geom g; const float* S; const float* rh; float* p; };
-struct ProlTask { TaskHead h; Geom gf, gc; float* pf; const float* pc; int ry, rz; };
+struct ProlTask { TaskHead h; Geom gf, gc; float* pf; const float* pc; int ry, rz; int b222; };
 struct UpdTask { TaskHead h; Geom g; double* x; const float* e; };
 
 // Claim virtual blocks of one step until its queue is empty.  The binary
@@ -189,7 +189,10 @@ __global__ void kb_dense(WALK_ARGS) {
 template <class T>
 __global__ void kb_prol(WALK_ARGS) {
     walk(t, n, total, ctr, st, ph, [](const ProlTask& k, const Blk& B) {
-        k_prolong_x2_blk<float>(k.gf, k.gc, k.pf, k.pc, k.ry, k.rz, B);
+        if (k.b222)
+            k_prolong_222_blk<float>(k.gf, k.gc, k.pf, k.pc, B);
+        else
+            k_prolong_x2_blk<float>(k.gf, k.gc, k.pf, k.pc, k.ry, k.rz, B);
     });
 }
 template <class T>
@@ -606,7 +609,10 @@ int build_steps(ples_mg_batch* b) {
                 t.pc = P(i, n + 1, 0);
                 t.ry = C.ry;
                 t.rz = C.rz;
-                B.add(t, prol_grid(F.g, C.g));
+                // eight fine cells per thread under full coarsening of even sizes
+                t.b222 = C.ry == 2 && C.rz == 2 && F.g.nx % 2 == 0 && F.g.ny % 2 == 0 && F.g.nz % 2 == 0;
+                B.add(t, t.b222 ? dim3((C.g.nx + 1 + 31) / 32, (F.g.ny + 10) / 8, (F.g.nz + 3) / 2)
+                                : prol_grid(F.g, C.g));
             }
             B.end();
             for (int s = 0; s < nupmax; ++s) line_steps(c, n, s, false, true);

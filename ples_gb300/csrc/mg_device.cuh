@@ -1311,6 +1311,60 @@ __global__ void k_prolong_x2(Geom gf, Geom gc, T* __restrict__ pf, const T* __re
     k_prolong_x2_blk<T>(gf, gc, pf, pc, ry, rz, hw_blk());
 }
 
+// Full coarsening (rx = ry = rz = 2): one thread makes the 2 x 2 x 2 fine
+// cells (2c..2c+1, 2cj..2cj+1, 2ck..2ck+1), which all interpolate the same
+// eight coarse values (c..c+1, cj..cj+1, ck..ck+1), ghosts included; each
+// fine cell gets the expressions of k_prolong_x2 in the same order.  nx, ny
+// and nz even, so the pairs cover the box and the coarse reads stay in the
+// coarse box.
+template <typename T>
+__device__ __forceinline__ void k_prolong_222_blk(Geom gf, Geom gc, T* __restrict__ pf, const T* __restrict__ pc,
+                                                  const Blk& B) {
+    const int c = B.x * blockDim.x + threadIdx.x;
+    const int cj = B.y * blockDim.y + threadIdx.y;
+    const int ck = B.z;
+    if (c > gc.nx || 2 * cj > gf.ny + 1) return;
+    const long long q = gc.at(c, cj, ck);
+    const int oj = (int)gc.sj, ok = (int)gc.sk;
+    const T p000 = pc[q], p100 = pc[q + 1], p010 = pc[q + oj], p110 = pc[q + oj + 1];
+    const T p001 = pc[q + ok], p101 = pc[q + ok + 1], p011 = pc[q + oj + ok], p111 = pc[q + oj + ok + 1];
+#pragma unroll
+    for (int dk = 0; dk < 2; ++dk) {
+        const int fk = 2 * ck + dk;
+        if (fk > gf.nz + 1) break;
+        const T wk0 = dk ? T(0.25) : T(0.75);
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj) {
+            const int fj = 2 * cj + dj;
+            if (fj > gf.ny + 1) break;
+            const T wj0 = dj ? T(0.25) : T(0.75);
+            T a = wj0 * wk0 * p000, bb = wj0 * wk0 * p100;
+            {
+                const T w = (T(1) - wj0) * wk0;
+                a += w * p010;
+                bb += w * p110;
+            }
+            {
+                const T w = wj0 * (T(1) - wk0);
+                a += w * p001;
+                bb += w * p101;
+                const T w2 = (T(1) - wj0) * (T(1) - wk0);
+                a += w2 * p011;
+                bb += w2 * p111;
+            }
+            // (scalar accesses: with i = 0 at element kOX = 31 of a row, the
+            // pair 2c, 2c+1 starts at an odd element)
+            T* f = pf + gf.at(2 * c, fj, fk);
+            f[0] = f[0] + (T(0.75) * a + T(0.25) * bb);
+            f[1] = f[1] + (T(0.25) * a + T(0.75) * bb);
+        }
+    }
+}
+template <typename T>
+__global__ void k_prolong_222(Geom gf, Geom gc, T* __restrict__ pf, const T* __restrict__ pc) {
+    k_prolong_222_blk<T>(gf, gc, pf, pc, hw_blk());
+}
+
 // ---------------------------------------------------------------------------
 // Exact solve on the coarsest level: e = S r with S the (pre-computed)
 // inverse of the bordered coarse system (interior cells and wall ghost rows

@@ -669,7 +669,10 @@ void vcycle(ples_mg_handle* h, bool zero_fine) {
         LevelData& F = h->L[n];
         LevelData& C = h->L[n + 1];
         timed_begin(h, KIND_PROLONG, n + 1);
-        if (C.rx == 2) {
+        if (C.rx == 2 && C.ry == 2 && C.rz == 2 && F.g.nx % 2 == 0 && F.g.ny % 2 == 0 && F.g.nz % 2 == 0) {
+            dim3 blk(32, 4), grd((C.g.nx + 1 + 31) / 32, (F.g.ny + 3 + 7) / 8, (F.g.nz + 3) / 2);
+            k_prolong_222<T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p);
+        } else if (C.rx == 2) {
             dim3 blk(32, 4), grd((C.g.nx + 1 + 31) / 32, (F.g.ny + 2 + 3) / 4, F.g.nz + 2);
             k_prolong_x2<T><<<grd, blk, 0, h->st>>>(F.g, C.g, (T*)F.p, (const T*)C.p, C.ry, C.rz);
         } else {
