@@ -1049,17 +1049,23 @@ double mean_spacing(const double* x, const double* y, const double* z, int jx, i
 // system singular.  Each column has kGjSlots keys, row r offering to slot
 // r mod kGjSlots (one address taking every row's atomic serialises the
 // step); the step that uses a column reduces its slots with one warp.
+// The matrix type R is FP64, or FP32 for a mixed handle, whose inverse is
+// stored in FP32 anyway (half the bytes per step; K and S then stay in L2).
 constexpr int kGjSlots = 32;
-__device__ __forceinline__ void gj_offer(unsigned long long* key, double v, int r, int m) {
-    if (v > 0.0)
-        atomicMax(key + r % kGjSlots,
-                  ((unsigned long long)(unsigned)__double2hiint(v) << 32) | (unsigned long long)(unsigned)(m - r));
+__device__ __forceinline__ unsigned gj_hi(double v) { return (unsigned)__double2hiint(v); }
+__device__ __forceinline__ unsigned gj_hi(float v) { return __float_as_uint(v); }
+template <typename R>
+__device__ __forceinline__ void gj_offer(unsigned long long* key, R v, int r, int m) {
+    if (v > R(0))
+        atomicMax(key + r % kGjSlots, ((unsigned long long)gj_hi(v) << 32) | (unsigned long long)(unsigned)(m - r));
 }
-__global__ void k_gj_first(const double* __restrict__ K, int m, unsigned long long* __restrict__ keys) {
+template <typename R>
+__global__ void k_gj_first(const R* __restrict__ K, int m, unsigned long long* __restrict__ keys) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < m) gj_offer(keys, fabs(K[(size_t)r * m]), r, m);
 }
-__global__ void k_gj_step(double* __restrict__ K, double* __restrict__ S, int m, int c,
+template <typename R>
+__global__ void k_gj_step(R* __restrict__ K, R* __restrict__ S, int m, int c,
                           unsigned long long* __restrict__ keys, int* __restrict__ used, int* __restrict__ pivrow,
                           int* __restrict__ bad) {
     __shared__ unsigned long long s_key;
@@ -1079,20 +1085,20 @@ __global__ void k_gj_step(double* __restrict__ K, double* __restrict__ S, int m,
         return;
     }
     const int p = m - (int)(unsigned)(key & 0xffffffffull);
-    double* Kr = K + (size_t)r * m;
-    double* Sr = S + (size_t)r * m;
+    R* Kr = K + (size_t)r * m;
+    R* Sr = S + (size_t)r * m;
     if (r == p) {
         if (threadIdx.x == 0) {
-            Sr[c] = 1.0;
+            Sr[c] = R(1);
             used[r] = 1;
             pivrow[c] = r;
         }
         return;
     }
-    const double* Kp = K + (size_t)p * m;
-    const double* Sp = S + (size_t)p * m;
-    const double f = Kr[c] / Kp[c];
-    if (f != 0.0) {
+    const R* Kp = K + (size_t)p * m;
+    const R* Sp = S + (size_t)p * m;
+    const R f = Kr[c] / Kp[c];
+    if (f != R(0)) {
         for (int q = c + 1 + (int)threadIdx.x; q < m; q += blockDim.x) Kr[q] -= f * Kp[q];
         for (int j = threadIdx.x; j < c; j += blockDim.x) Sr[j] -= f * Sp[j];
         if (threadIdx.x == 0) Sr[c] = -f;
@@ -1103,8 +1109,8 @@ __global__ void k_gj_step(double* __restrict__ K, double* __restrict__ S, int m,
 // the inverse of the bordered system without its border: row c of the
 // inverse is row pivrow[c] of S over its pivot, column j of S is unknown
 // pivrow[j]
-template <typename T>
-__global__ void k_gj_extract(const double* __restrict__ K, const double* __restrict__ S,
+template <typename R, typename T>
+__global__ void k_gj_extract(const R* __restrict__ K, const R* __restrict__ S,
                              const int* __restrict__ pivrow, int m, int n, T* __restrict__ out) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
@@ -1228,22 +1234,28 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         tmp.push_back(*p);
         return PLES_MG_OK;
     };
-    double *dK, *dI;
+    // the elimination runs in the type of the stored inverse
+    using R = T;
+    double* dK64;
+    R *dK, *dI;
     unsigned long long* dKey;
     int *dUsed, *dPiv, *dBad;
     int rc;
-    if ((rc = talloc((void**)&dK, 8 * (size_t)m * m)) || (rc = talloc((void**)&dI, 8 * (size_t)m * m)) ||
+    if ((rc = talloc((void**)&dK64, 8 * (size_t)m * m)) ||
+        (rc = talloc((void**)&dK, sizeof(R) * (size_t)m * m)) || (rc = talloc((void**)&dI, sizeof(R) * (size_t)m * m)) ||
         (rc = talloc((void**)&dKey, 8 * ((size_t)m + 1) * kGjSlots)) || (rc = talloc((void**)&dUsed, sizeof(int) * (size_t)m)) ||
         (rc = talloc((void**)&dPiv, sizeof(int) * (size_t)m)) || (rc = talloc((void**)&dBad, sizeof(int))))
         return rc;
     auto gj = [&]() -> int {
-        CK(cudaMemcpyAsync(dK, K.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
-        CK(cudaMemsetAsync(dI, 0, 8 * (size_t)m * m, h->st));
+        CK(cudaMemcpyAsync(dK64, K.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
+        k_convert<R, double><<<grid1((long long)m * m), 256, 0, h->st>>>((long long)m * m, dK64, dK);
+        CK(cudaMemsetAsync(dI, 0, sizeof(R) * (size_t)m * m, h->st));
         CK(cudaMemsetAsync(dKey, 0, 8 * ((size_t)m + 1) * kGjSlots, h->st));
         CK(cudaMemsetAsync(dUsed, 0, sizeof(int) * (size_t)m, h->st));
         CK(cudaMemsetAsync(dBad, 0, sizeof(int), h->st));
-        k_gj_first<<<(m + 255) / 256, 256, 0, h->st>>>(dK, m, dKey);
-        for (int col = 0; col < m; ++col) k_gj_step<<<m, 256, 0, h->st>>>(dK, dI, m, col, dKey, dUsed, dPiv, dBad);
+        k_gj_first<R><<<(m + 255) / 256, 256, 0, h->st>>>(dK, m, dKey);
+        for (int col = 0; col < m; ++col)
+            k_gj_step<R><<<m, 256, 0, h->st>>>(dK, dI, m, col, dKey, dUsed, dPiv, dBad);
         h->launches += 1LL + m;
         CK(cudaGetLastError());
         int hbad = 0;
@@ -1251,7 +1263,7 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         CK(cudaStreamSynchronize(h->st));
         if (hbad) return fail(h, PLES_MG_BAD_ARG, "coarsest-level system is singular");
         if ((rc = dalloc(h, &h->coarse_S, sizeof(T) * (size_t)n * n))) return rc;
-        k_gj_extract<T><<<dim3((m + 255) / 256, n), 256, 0, h->st>>>(dK, dI, dPiv, m, n, (T*)h->coarse_S);
+        k_gj_extract<R, T><<<dim3((m + 255) / 256, n), 256, 0, h->st>>>(dK, dI, dPiv, m, n, (T*)h->coarse_S);
         ++h->launches;
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(h->st));
