@@ -69,12 +69,12 @@ struct TaskHead {
 };
 struct GhostTask { TaskHead h; Geom g; double* p; };
 struct SumTask { TaskHead h; Geom g; const double* a; double* part; int squares; };
-struct RedTask { TaskHead h; int mode; const double* pa; const double* pb; long long n; double ncell; };
+struct RedTask { TaskHead h; int mode; const double* pa; const double* pb; long long n; double ncell; int* sc; int oc; };
 struct AddTask { TaskHead h; Geom g; double* a; int box; int use_mean; const uint8_t* solid; };
 struct ZeroTask { TaskHead h; Geom g; double* a; const uint8_t* solid; };
 struct WallCTask { TaskHead h; Geom g; Coef<double> c; const double* p; double* w; };
 struct WallSTask { TaskHead h; Geom g; double* p; const double* w; };
-struct RoutTask { TaskHead h; Geom g; Coef<double> c; const double* x; const double* b; float* rin; double* psq; double* pmax; const uint8_t* tipo; };
+struct RoutTask { TaskHead h; Geom g; Coef<float2> cs; const int* sc; const double* x; const double* b; float* rin; double* psq; double* pmax; const uint8_t* tipo; };
 struct LineTask { TaskHead h; Geom g; Coef<float> c; const float* cp; const float* pin; const float* pk; float* pout; const float* rh; float omega; int kpar; int zk; int wide; };
 struct RRTask { TaskHead h; Geom gf, gc; Coef<float> c; const float* p; const float* rh; float* rhc; int rx, ry, rz; };
 struct DenseTask { TaskHead h; Geom g; const float* S; const float* rh; float* p; };
@@ -153,10 +153,12 @@ template <class T>
 __global__ void kb_walls(WALK_ARGS) {
     walk(t, n, total, ctr, st, ph, [](const WallSTask& k, const Blk& B) { k_wall_scatter_blk(k.g, k.p, k.w, B); });
 }
+// the outer residual of the (mixed) members in double-float, as the
+// single-grid solve forms it
 template <class T>
-__global__ void __launch_bounds__(256) kb_rout(WALK_ARGS) {
+__global__ void __launch_bounds__(256, 4) kb_rout(WALK_ARGS) {
     walk(t, n, total, ctr, st, ph, [](const RoutTask& k, const Blk& B) {
-        k_resid_outer2_blk<float, 8>(k.g, k.c, k.x, k.b, k.rin, k.psq, k.pmax, B, k.tipo);
+        k_resid_outer2_df_blk<float, 8>(k.g, k.cs, k.x, k.b, k.rin, k.psq, k.pmax, B, k.tipo, k.sc);
     });
 }
 template <class T, bool ZIN>
@@ -218,6 +220,12 @@ __global__ void kb_red(WALK_ARGS) {
             case RED_BNORM:
                 S.bn2 = s;
                 S.bnorm = s > 0.0 ? sqrt(s) : 1.0;
+                if (k.sc) {  // scale of the double-float residual: b's RMS into [1, 2)
+                    const double rms = sqrt(s / k.ncell);
+                    const int ob = rms > 0.0 && isfinite(rms) ? min(100, max(-100, -ilogb(rms))) : 0;
+                    k.sc[0] = ob;
+                    k.sc[1] = ob - k.oc;
+                }
                 S.it = 0;
                 S.vcycles = 0;
                 S.rel0 = -1.0;
@@ -404,6 +412,10 @@ int build_steps(ples_mg_batch* b) {
             RedTask t{};
             t.h.inst = i;
             t.mode = mode;
+            if (mode == RED_BNORM && h->L[0].has_cs) {
+                t.sc = h->dscale;
+                t.oc = h->oc;
+            }
             t.ncell = h->masked ? (double)h->nfluid : (double)g.nx * g.ny * g.nz;
             if (src == 0) {
                 const dim3 r = red_grid2(g);
@@ -544,7 +556,8 @@ int build_steps(ples_mg_batch* b) {
         RoutTask t{};
         t.h.inst = i;
         t.g = h->L[0].g;
-        t.c = h->L[0].cd;
+        t.cs = h->L[0].cs;
+        t.sc = h->dscale;
         t.x = h->x;
         t.b = h->b;
         t.rin = (float*)h->L[0].rh;
