@@ -1388,7 +1388,24 @@ __device__ __forceinline__ void k_dense_solve_blk(Geom g, const T* __restrict__ 
     if (u >= n) return;
     const T* row = S + (long long)u * n;
     T s = T(0);
-    for (int v = lane; v < n; v += 32) s += row[v] * r[v];
+    if (sizeof(T) == 4 && (n & 3) == 0) {
+        // FP32 rows of a multiple of 4 entries start on 16-byte boundaries:
+        // 16-byte loads (S is read once per solve: streaming) and four
+        // independent accumulators
+        const float4* row4 = reinterpret_cast<const float4*>(row);
+        const float4* r4 = reinterpret_cast<const float4*>(r);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+        for (int v = lane; v < (n >> 2); v += 32) {
+            const float4 a = __ldcs(row4 + v), b = r4[v];
+            a0 += a.x * b.x;
+            a1 += a.y * b.y;
+            a2 += a.z * b.z;
+            a3 += a.w * b.w;
+        }
+        s = T((a0 + a1) + (a2 + a3));
+    } else {
+        for (int v = lane; v < n; v += 32) s += row[v] * r[v];
+    }
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) {
         const int j = u % nj, col = u / nj;
