@@ -308,10 +308,14 @@ int ples_mg_get_line_threads(const ples_mg_handle *h, int level, int *threads);
 
 /* ---- many grids at once ------------------------------------------------
  * No counterpart in the reference, which solves one grid per run.  A batch
- * groups existing handles (mixed precision, zebra smoother, full
- * coarsening, periodic x and z, a dense coarsest level,
- * all on one device; immersed-boundary masks and cell types allowed); each
- * keeps its resident hierarchy.  One outer iteration of all members is a captured
+ * groups existing handles on one device; each keeps its resident hierarchy.
+ * Members with mixed precision, the zebra smoother, full coarsening,
+ * periodic x and z and a dense coarsest level (immersed-boundary masks and
+ * cell types allowed) share the batched step list; any other member (x or
+ * z walls, FP64, another smoother, semi-coarsening) is solved by the
+ * single-grid solver within the same call, after the batched members, and
+ * the server solves such a member's requests when it admits them.  One
+ * outer iteration of the batched members is a captured
  * CUDA graph of persistent step kernels that walk (member, level, tile)
  * queues; convergence is decided per member on the device, so members of
  * different sizes finish independently.  The stop rule is the relative one

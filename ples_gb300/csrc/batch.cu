@@ -291,6 +291,10 @@ struct Step {
 // The engine: members, their step list, the task tables and the graph.
 struct ples_mg_batch {
     std::vector<ples_mg_handle*> mem;
+    // members the step list does not cover (x / z walls, FP64, another
+    // smoother, semi-coarsening, no dense coarsest level): solved one after
+    // another by the single-grid solver within the same call
+    std::vector<char> solo;
     int dev = 0, nsm = 0;
     cudaStream_t st = nullptr;
     InstState* d_state = nullptr;
@@ -340,6 +344,7 @@ struct Builder {
     }
     template <class Task>
     void add(Task t, dim3 grid) {
+        if (b->solo[t.h.inst]) return;  // solved outside the step list
         t.h.blk0 = cur.total;
         t.h.gx = (int)grid.x;
         t.h.gy = (int)grid.y;
@@ -368,7 +373,7 @@ int build_steps(ples_mg_batch* b) {
     // kb_line_wide runs the 64-line form or the 32-line form with 16 warps:
     // its shared memory is the larger of the two over all members' levels
     for (int i = 0; i < nm; ++i)
-        for (int n = 0; n < b->mem[i]->nlev; ++n) {
+        for (int n = 0; n < b->mem[i]->nlev && !b->solo[i]; ++n) {
             const size_t ny2 = (size_t)b->mem[i]->L[n].g.ny + 2;
             b->smem_wide = std::max(b->smem_wide, std::max(3 * ny2 * 64 + 4 * 16 * 32, (3 * ny2 + 4 * 16) * 32) *
                                                       sizeof(float));
@@ -380,6 +385,7 @@ int build_steps(ples_mg_batch* b) {
     for (int i = 0; i < nm; ++i) {
         ples_mg_handle* h = b->mem[i];
         cur[i].assign(h->nlev, 0);
+        if (b->solo[i]) continue;
         lmax = std::max(lmax, h->nlev);
         numax = std::max(numax, h->nu_pre);
         nupmax = std::max(nupmax, h->nu_post);
@@ -652,12 +658,13 @@ int build_steps(ples_mg_batch* b) {
     red_step(PH_EPI, RED_FINISH, 2);
 
     for (int i = 0; i < nm; ++i)
-        for (int n = 0; n < (int)cur[i].size(); ++n)
+        for (int n = 0; n < (int)cur[i].size() && !b->solo[i]; ++n)
             if (cur[i][n] != 0)
                 return bfail(b, PLES_MG_BAD_ARG, "member %d: odd sweep count per outer iteration on level %d", i,
                              n + 1);
     for (int i = 0; i < nm; ++i) {
         ples_mg_handle* h = b->mem[i];
+        if (b->solo[i]) continue;
         for (int n = 0; n < h->nlev; ++n)
             b->smem_line = std::max(b->smem_line, (3 * (size_t)(h->L[n].g.ny + 2) + 4 * 8) * 32 * sizeof(float));
         b->smem_dense = std::max(b->smem_dense, (size_t)h->coarse_n * sizeof(float));
@@ -725,15 +732,14 @@ int batch_create(ples_mg_handle* const* members, int n, ples_mg_batch* b) {
     for (int i = 0; i < n; ++i) {
         ples_mg_handle* h = members[i];
         if (!h) return bfail(b, PLES_MG_BAD_ARG, "member %d is null", i);
-        if (h->d.precision != PLES_MG_PREC_MIXED || h->smoother != 0 || h->d.coarsening != 0)
-            return bfail(b, PLES_MG_BAD_ARG,
-                         "member %d: batched solves need mixed precision, the zebra smoother and full coarsening", i);
-        if (!h->coarse_S) return bfail(b, PLES_MG_BAD_ARG, "member %d: coarsest level too large for the dense solve", i);
-        if (h->walls_xz) return bfail(b, PLES_MG_BAD_ARG, "member %d: x or z walls are not batched", i);
-        for (int l = 1; l < h->nlev; ++l)
-            if (h->L[l].rx != 2) return bfail(b, PLES_MG_BAD_ARG, "member %d: level %d not coarsened in x", i, l + 1);
         if (h->dev != members[0]->dev) return bfail(b, PLES_MG_BAD_ARG, "members live on different devices");
+        // the step list covers mixed precision, the zebra smoother, full
+        // coarsening in x, periodic x and z and a dense coarsest level
+        bool solo = h->d.precision != PLES_MG_PREC_MIXED || h->smoother != 0 || h->d.coarsening != 0 ||
+                    !h->coarse_S || h->walls_xz;
+        for (int l = 1; l < h->nlev; ++l) solo = solo || h->L[l].rx != 2;
         b->mem.push_back(h);
+        b->solo.push_back(solo ? 1 : 0);
     }
     b->dev = members[0]->dev;
     BK(cudaSetDevice(b->dev));
@@ -865,27 +871,48 @@ int batch_solve(ples_mg_batch* b, double* const* fi, const double* const* rhs, d
     BK(cudaSetDevice(b->dev));
     for (int i = 0; i < nm; ++i) {
         if (!rhs[i]) return bfail(b, PLES_MG_BAD_ARG, "rhs of member %d is null", i);
+        if (b->solo[i]) continue;
         int rc = stage_in(b, i, fi ? fi[i] : nullptr, rhs[i], device_ptrs);
         if (rc) return rc;
         admit(b, i, rel_tol, abs_tol, max_cycles);
     }
     int rc = push_state(b);
     if (rc) return rc;
-    for (long long r = 0; r < (long long)max_cycles + 3; ++r) {
+    bool any = false;
+    for (int i = 0; i < nm; ++i) any = any || !b->solo[i];
+    for (long long r = 0; any && r < (long long)max_cycles + 3; ++r) {
         if ((rc = replay(b))) return rc;
         bool all = true;
-        for (int i = 0; i < nm; ++i) all = all && b->h_state[i].phase == PH_DONE;
+        for (int i = 0; i < nm; ++i) all = all && (b->solo[i] || b->h_state[i].phase == PH_DONE);
         if (all) break;
     }
     int worst = PLES_MG_OK;
+    auto fold = [&](int s) {
+        if (s == PLES_MG_DIVERGED) worst = s;
+        else if (s == PLES_MG_NOT_CONVERGED && worst == PLES_MG_OK) worst = s;
+    };
+    // the members outside the step list, one after another
     for (int i = 0; i < nm; ++i) {
+        if (!b->solo[i]) continue;
+        ples_mg_handle* h = b->mem[i];
+        if ((rc = stage_in(b, i, fi ? fi[i] : nullptr, rhs[i], device_ptrs))) return rc;
+        BK(cudaStreamSynchronize(b->st));
+        ples_mg_stats st{};
+        const int s = solve_resident(h, rel_tol, abs_tol, max_cycles, &st);
+        if (s != PLES_MG_OK && s != PLES_MG_NOT_CONVERGED && s != PLES_MG_DIVERGED)
+            return bfail(b, s, "member %d: %s", i, h->err.c_str());
+        BK(cudaStreamSynchronize(h->st));
+        if (fi && fi[i] && (rc = stage_out(b, i, fi[i], device_ptrs))) return rc;
+        if (stats) stats[i] = st;
+        fold(s);
+    }
+    for (int i = 0; i < nm; ++i) {
+        if (b->solo[i]) continue;
         if (b->h_state[i].phase != PH_DONE)
             return bfail(b, PLES_MG_CUDA_ERROR, "member %d did not finish (phase %d)", i, b->h_state[i].phase);
         if (fi && fi[i] && (rc = stage_out(b, i, fi[i], device_ptrs))) return rc;
         if (stats) to_stats(b->h_state[i], &stats[i]);
-        const int s = b->h_state[i].status;
-        if (s == PLES_MG_DIVERGED) worst = s;
-        else if (s == PLES_MG_NOT_CONVERGED && worst == PLES_MG_OK) worst = s;
+        fold(b->h_state[i].status);
         b->h_state[i].phase = PH_IDLE;
     }
     if ((rc = push_state(b))) return rc;
@@ -998,6 +1025,31 @@ void srv_loop(ples_srv* s) {
             const int i = r->member;
             std::memcpy(s->pin_rhs[i], r->rhs.data(), sizeof(double) * r->rhs.size());
             if ((rc = stage_in(b, i, nullptr, s->pin_rhs[i], false))) break;
+            if (b->solo[i]) {  // outside the step list: solved now, warm-started from its last solution
+                ples_mg_handle* h = b->mem[i];
+                if (cudaStreamSynchronize(b->st) != cudaSuccess) { rc = PLES_MG_CUDA_ERROR; break; }
+                ples_mg_stats st{};
+                const int sr = solve_resident(h, r->rel_tol, 0.0, r->max_cycles, &st);
+                if (sr != PLES_MG_OK && sr != PLES_MG_NOT_CONVERGED && sr != PLES_MG_DIVERGED) { rc = sr; break; }
+                if (cudaStreamSynchronize(h->st) != cudaSuccess || (rc = stage_out(b, i, s->pin_fi[i], false)) ||
+                    cudaStreamSynchronize(b->st) != cudaSuccess) {
+                    rc = rc ? rc : PLES_MG_CUDA_ERROR;
+                    break;
+                }
+                const auto now = std::chrono::steady_clock::now();
+                std::lock_guard<std::mutex> lk(s->mu);
+                if (r->fi_out) std::memcpy(r->fi_out, s->pin_fi[i], sizeof(double) * box_count(h->L[0].g));
+                r->st = st;
+                r->st.seconds = std::chrono::duration<double>(now - r->t_sub).count();
+                r->rc = sr;
+                r->done = true;
+                s->lat_ms.push_back(r->st.seconds * 1e3);
+                ++s->completed;
+                s->finished.push_back(r);
+                s->inflight[i].reset();
+                s->cv_done.notify_all();
+                continue;
+            }
             admit(b, i, r->rel_tol, 0.0, r->max_cycles);
             dirty = true;
         }

@@ -131,3 +131,8 @@ inline int fail(ples_mg_handle* h, int code, const char* fmt, ...) {
             return fail(h, e_ == cudaErrorMemoryAllocation ? PLES_MG_OOM : PLES_MG_CUDA_ERROR, \
                         "%s failed: %s", #call, cudaGetErrorString(e_));                       \
     } while (0)
+
+namespace ples {
+// single-grid solve from the resident boxes, no wall fluxes (ples_mg.cu)
+int solve_resident(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles, ples_mg_stats* st);
+}  // namespace ples

@@ -1706,6 +1706,18 @@ int get_box(ples_mg_handle* h, const Geom& g, int ghost, const double* box, doub
 
 // ===========================================================================
 // C ABI
+namespace ples {
+// A solve of a handle from its resident boxes (x the initial guess with its
+// ghosts, b the right-hand side) with no wall fluxes: what a batch or the
+// server runs for a member its step list does not cover.  The caller has
+// set the device and staged x and b on a stream it has synchronised.
+int solve_resident(ples_mg_handle* h, double rel_tol, double abs_tol, int max_cycles, ples_mg_stats* st) {
+    int rc = upload_cs(h, nullptr, false);
+    if (rc) return rc;
+    return solve_any(h, rel_tol, abs_tol, max_cycles, st);
+}
+}  // namespace ples
+
 extern "C" {
 
 int ples_mg_create(const ples_mg_desc* desc, ples_mg_handle** out) {

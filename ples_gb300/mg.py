@@ -440,8 +440,10 @@ def _ptr_array(ptrs):
 
 class Batch:
     """Many grids solved together (ples_mg_batch_*): the members are
-    Multigrid objects (mixed precision, zebra smoother, full coarsening)
-    that keep their resident hierarchies."""
+    Multigrid objects that keep their resident hierarchies.  Mixed-precision
+    members with the zebra smoother, full coarsening, periodic x and z and a
+    dense coarsest level share the batched step list; any other member is
+    solved by the single-grid solver within the same call."""
 
     def __init__(self, members):
         self._L = load()

@@ -73,11 +73,40 @@ def test_batch_matches_single_solves_and_oracle(cases):
         m.close()
 
 
-def test_batch_rejects_unsupported_members(cases):
-    x, y, z, _ = cases[0]
-    with mg.Multigrid(x, y, z, precision="fp64") as m:
-        with pytest.raises(mg.PlesMGError):
-            mg.Batch([m])
+def test_batch_with_members_outside_the_step_list(cases):
+    """FP64, x-walled and point-SOR members join a batch with a plain one:
+    the step list covers the plain member and the others are solved one
+    after another by the single-grid solver within the same call, so their
+    fields are the ones a single solve gives, bit for bit, and the plain
+    member's agrees with its single solve within 1e-9."""
+    x, y, z, rhs = cases[0]
+    xw, yw, zw = S.wavy_channel_grid(32, 16, 32, 0.05, 2.0)  # walls need a grid whose x relation contracts
+    rw = S.divergence_rhs(32, 16, 32, seed=61)
+    xp, yp, zp = S.wavy_channel_grid(32, 16, 32, 0.03, 1.3)  # mild stretching for the point smoother
+    rp = S.divergence_rhs(32, 16, 32, seed=62)
+    members = [mg.Multigrid(x, y, z), mg.Multigrid(x, y, z, precision="fp64"), mg.Multigrid(xw, yw, zw, ip=1),
+               mg.Multigrid(xp, yp, zp, smoother=3)]
+    rhs_l = [rhs, rhs, rw, rp]
+    try:
+        singles = [m.solve(r, rel_tol=REL_TOL) for m, r in zip(members, rhs_l)]
+        with mg.Batch(members) as b:
+            fis, sts = b.solve(rhs_l, rel_tol=REL_TOL)
+        for i, ((fs, ss), fb, sb) in enumerate(zip(singles, fis, sts)):
+            assert sb["status"] == mg.OK and sb["rel_residual"] <= REL_TOL, (i, sb)
+            if i == 0:
+                assert np.abs(fb - fs).max() <= 1e-9 * np.abs(fs).max()
+            else:
+                np.testing.assert_array_equal(fb, fs)
+                assert sb["outer_iterations"] == ss["outer_iterations"]
+        # the server takes them too: a request to the walled member (warm
+        # start from its last solution) gives its single solve
+        with mg.Server(members[:3]) as s:
+            fo, so = s.wait(s.submit(2, rw, rel_tol=REL_TOL))
+        assert so["status"] == mg.OK
+        assert np.abs(fo - singles[2][0]).max() <= 1e-9 * np.abs(singles[2][0]).max()
+    finally:
+        for m in members:
+            m.close()
 
 
 def test_batch_with_masked_and_typed_members():

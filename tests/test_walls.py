@@ -108,12 +108,19 @@ def test_wall_fluxes_on_x_and_z_walls(grid):
     assert l2 <= 1e-8 and mx <= 1e-8, (l2, mx)
 
 
-def test_walls_rejected_where_unsupported(grid):
+def test_walls_in_a_batch_and_rejected_with_a_mask(grid):
+    """A walled member of a batch is solved by the single-grid solver within
+    the batch call (the same field as its own solve); walls and an
+    immersed-boundary mask together are rejected at creation."""
     from ples_gb300 import mg
     x, y, z = grid
+    rhs = S.divergence_rhs(*DIMS, seed=9)
     with mg.Multigrid(x, y, z, ip=1) as m:
-        with pytest.raises(mg.PlesMGError):
-            mg.Batch([m])
+        fs, ss = m.solve(rhs, rel_tol=1e-10)
+        with mg.Batch([m]) as b:
+            (fb,), (sb,) = b.solve([rhs], rel_tol=1e-10)
+    assert ss["status"] == mg.OK and sb["status"] == mg.OK
+    np.testing.assert_array_equal(fb, fs)
     with pytest.raises(mg.PlesMGError):
         mg.Multigrid(x, y, z, kp=1, solid=np.zeros(DIMS, dtype=bool))
 
