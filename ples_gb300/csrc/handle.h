@@ -65,6 +65,7 @@ struct ples_mg_handle {
     int* dflag = nullptr;                                // bounded-wait error flag, inside red
     int* dscale = nullptr;                               // ob, ox of the double-float residual (inside red)
     int oc = 0;                                          // power-of-two scale of the split coefficients
+    bool probe_fallback = false;                         // the default settings diverged on this grid (earlier defaults taken)
     int* x2sync = nullptr;                               // tickets and plane counters of k_line_relax_x2m (nz + 3)
     unsigned wait_polls = ples::kSpinLimit;              // polls of a bounded device wait before it gives up
     double* h_red = nullptr;                             // pinned host copy
