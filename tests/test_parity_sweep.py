@@ -1,8 +1,9 @@
 """A seeded sweep of small problems against the oracle, through the C ABI.
 
 Each case draws its size, wall amplitude and stretching, walls in x and z,
-the smoother (zebra line SOR or the multicolour point SOR, with or without a
-free surface), the precision and the level count.  The device solve to
+the smoother (zebra line SOR, eta-line Jacobi, zebra with TMA-staged rows,
+or the multicolour point SOR with or without a free surface), the
+precision, the level count and full or semi-coarsening.  The device solve to
 ||r||/||b|| <= 1e-12 agrees with the oracle's converged solution (eps 1e-13)
 within 1e-8 in the L2 and max norms: of the zero-mean fields, or of the
 fields themselves with a free surface (which fixes the pressure level).
@@ -30,6 +31,10 @@ def _draw(seed):
     walls = rng.random() < 0.4
     point = not walls and rng.random() < 0.35
     mild = walls or point
+    # the line smoother's other forms: eta-line Jacobi, rows staged by TMA
+    # (FP32, periodic); semi-coarsening of the hierarchy
+    other = 0 if point else int(rng.choice([0, 0, 0, 1, 2]))
+    coarsening = int(rng.random() < 0.3)
     amp = float(rng.uniform(0.0, 0.05 if mild else 0.12))
     beta = float(rng.uniform(1.2, 1.8 if mild else 2.6))
     ip = kp = 0
@@ -41,8 +46,11 @@ def _draw(seed):
         if not ip and not kp:
             ip = 1
     fs = point and rng.random() < 0.5
-    return dict(dims=dims, amp=amp, beta=beta, ip=ip, kp=kp, smoother=3 if point else 0, fs=fs,
-                precision=("mixed", "fp64")[int(rng.integers(2))], nlevmax=(0, 4)[int(rng.integers(2))],
+    precision = ("mixed", "fp64")[int(rng.integers(2))]
+    if other == 2:  # the TMA-staged rows are FP32 and periodic only
+        other, precision = (0, precision) if walls else (2, "mixed")
+    return dict(dims=dims, amp=amp, beta=beta, ip=ip, kp=kp, smoother=3 if point else other, fs=fs,
+                precision=precision, nlevmax=(0, 4)[int(rng.integers(2))], coarsening=coarsening,
                 seed=int(rng.integers(1 << 30)))
 
 
@@ -50,7 +58,7 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b), np.abs(a - b).max() / np.abs(b).max()
 
 
-@pytest.mark.parametrize("case", range(16))
+@pytest.mark.parametrize("case", range(24))
 def test_random_problem_against_the_oracle(case):
     c = _draw(case)
     jx, jy, jz = c["dims"]
@@ -65,7 +73,8 @@ def test_random_problem_against_the_oracle(case):
         orc.set_free_surface(True, prs)
     fo, _, _, rr = orc.multi(rhs, eps=1e-13, ficycle=3000)
     assert rr <= 1e-13, (c, rr)
-    kw = dict(ip=c["ip"], kp=c["kp"], precision=c["precision"], smoother=c["smoother"], nlevmax=c["nlevmax"])
+    kw = dict(ip=c["ip"], kp=c["kp"], precision=c["precision"], smoother=c["smoother"], nlevmax=c["nlevmax"],
+              coarsening=c["coarsening"])
     if c["fs"]:
         kw["freesurface"] = 1
     with mg.Multigrid(x, y, z, **kw) as m:
