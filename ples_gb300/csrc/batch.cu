@@ -953,7 +953,9 @@ struct ples_srv {
         bool done = false;
     };
     std::deque<std::shared_ptr<Req>> pending;
-    std::vector<std::shared_ptr<Req>> inflight;  // per member
+    std::vector<std::shared_ptr<Req>> inflight;  // per member: admitted, solving
+    std::vector<std::shared_ptr<Req>> prepared;  // per member: next request, its rhs in pin_rhs
+    std::vector<std::shared_ptr<Req>> handing;   // per member: finished, solution being copied out
     std::vector<std::shared_ptr<Req>> finished;  // not yet collected by wait
     std::vector<double*> pin_rhs, pin_fi;        // per-member pinned staging
     cudaEvent_t ev_out = nullptr;
@@ -975,13 +977,14 @@ size_t rhs_count(const Geom& g) { return (size_t)g.nx * g.ny * g.nz; }
 void srv_fail_all(ples_srv* s, int rc) {  // under s->mu
     s->fatal = rc;
     s->err = s->eng->err;
-    for (auto& r : s->inflight)
-        if (r) {
-            r->rc = rc;
-            r->done = true;
-            s->finished.push_back(r);
-            r.reset();
-        }
+    for (auto* v : {&s->inflight, &s->prepared, &s->handing})
+        for (auto& r : *v)
+            if (r) {
+                r->rc = rc;
+                r->done = true;
+                s->finished.push_back(r);
+                r.reset();
+            }
     for (auto& r : s->pending) {
         r->rc = rc;
         r->done = true;
@@ -992,20 +995,42 @@ void srv_fail_all(ples_srv* s, int rc) {  // under s->mu
     s->cv_done.notify_all();
 }
 
+// The worker.  Per member: inflight (admitted, solving), prepared (its
+// right-hand side already in the member's pinned buffer, admitted as soon as
+// the member finishes) and handing (finished, its solution being copied
+// out).  One pass: admit requests of idle members, replay once, and while
+// the replay runs hand out the solutions copied before it and copy the next
+// requests' right-hand sides into pinned memory; after it, a finished
+// member's solution is queued for copy-out and its prepared request admitted
+// at once, so it joins the next replay (warm-started from the solution just
+// copied out: the copy is queued first on the same stream).
 void srv_loop(ples_srv* s) {
     ples_mg_batch* b = s->eng;
     const int nm = (int)b->mem.size();
     cudaSetDevice(b->dev);
     std::vector<int> out_pending;  // copy-out enqueued before the current replay
     std::vector<ples_mg_stats> snap(nm);
+    // a stage-in from pin_rhs[i] is queued and may not have run yet (cleared
+    // by the stream synchronisation after each replay)
+    std::vector<char> rhs_busy(nm, 0);
     bool dirty = false;            // host-side phase changes not yet on the device
+    auto finish = [&](const std::shared_ptr<ples_srv::Req>& r, const ples_mg_stats& st, int rc,
+                      std::chrono::steady_clock::time_point now) {  // under s->mu
+        r->st = st;
+        r->st.seconds = std::chrono::duration<double>(now - r->t_sub).count();
+        r->rc = rc;
+        r->done = true;
+        s->lat_ms.push_back(r->st.seconds * 1e3);
+        ++s->completed;
+        s->finished.push_back(r);
+    };
     for (;;) {
         std::vector<std::shared_ptr<ples_srv::Req>> admit_now;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             auto busy = [&] {
                 for (int i = 0; i < nm; ++i)
-                    if (s->inflight[i]) return true;
+                    if (s->inflight[i] || s->handing[i] || s->prepared[i]) return true;
                 return false;
             };
             s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty() || busy(); });
@@ -1025,6 +1050,7 @@ void srv_loop(ples_srv* s) {
             const int i = r->member;
             std::memcpy(s->pin_rhs[i], r->rhs.data(), sizeof(double) * r->rhs.size());
             if ((rc = stage_in(b, i, nullptr, s->pin_rhs[i], false))) break;
+            rhs_busy[i] = 1;
             if (b->solo[i]) {  // outside the step list: solved now, warm-started from its last solution
                 ples_mg_handle* h = b->mem[i];
                 if (cudaStreamSynchronize(b->st) != cudaSuccess) { rc = PLES_MG_CUDA_ERROR; break; }
@@ -1039,13 +1065,7 @@ void srv_loop(ples_srv* s) {
                 const auto now = std::chrono::steady_clock::now();
                 std::lock_guard<std::mutex> lk(s->mu);
                 if (r->fi_out) std::memcpy(r->fi_out, s->pin_fi[i], sizeof(double) * box_count(h->L[0].g));
-                r->st = st;
-                r->st.seconds = std::chrono::duration<double>(now - r->t_sub).count();
-                r->rc = sr;
-                r->done = true;
-                s->lat_ms.push_back(r->st.seconds * 1e3);
-                ++s->completed;
-                s->finished.push_back(r);
+                finish(r, st, sr, now);
                 s->inflight[i].reset();
                 s->cv_done.notify_all();
                 continue;
@@ -1063,30 +1083,44 @@ void srv_loop(ples_srv* s) {
             active = active || ph == PH_PRO || ph == PH_ITER || ph == PH_EPI;
         }
         if (!rc && active && cudaGraphLaunch(b->exec, b->st) != cudaSuccess) rc = PLES_MG_CUDA_ERROR;
-        // while the replay runs: hand out the results copied before it
+        // while the replay runs: hand out the results copied before it ...
         if (!rc && !out_pending.empty()) {
             if (cudaEventSynchronize(s->ev_out) != cudaSuccess) rc = PLES_MG_CUDA_ERROR;
             const auto now = std::chrono::steady_clock::now();
             std::lock_guard<std::mutex> lk(s->mu);
             for (int i : out_pending) {
-                auto r = s->inflight[i];
+                auto r = s->handing[i];
                 if (!rc && r->fi_out) std::memcpy(r->fi_out, s->pin_fi[i], sizeof(double) * box_count(b->mem[i]->L[0].g));
-                r->st = snap[i];
-                r->st.seconds = std::chrono::duration<double>(now - r->t_sub).count();
-                r->rc = rc ? rc : r->st.status;
-                r->done = true;
-                s->lat_ms.push_back(r->st.seconds * 1e3);
-                ++s->completed;
-                s->finished.push_back(r);
-                s->inflight[i].reset();
+                finish(r, snap[i], rc ? rc : snap[i].status, now);
+                s->handing[i].reset();
             }
             s->cv_done.notify_all();
             out_pending.clear();
         }
+        // ... and stage the next request of each busy member in pinned memory
+        if (!rc) {
+            std::vector<std::shared_ptr<ples_srv::Req>> prep;
+            {
+                std::lock_guard<std::mutex> lk(s->mu);
+                for (auto it = s->pending.begin(); it != s->pending.end();) {
+                    const int i = (*it)->member;
+                    if (!b->solo[i] && s->inflight[i] && !s->prepared[i] && !rhs_busy[i]) {
+                        s->prepared[i] = *it;
+                        prep.push_back(*it);
+                        it = s->pending.erase(it);
+                    } else {
+                        ++it;
+                    }
+                }
+            }
+            for (auto& r : prep) std::memcpy(s->pin_rhs[r->member], r->rhs.data(), sizeof(double) * r->rhs.size());
+        }
         if (!rc && cudaStreamSynchronize(b->st) != cudaSuccess) rc = PLES_MG_CUDA_ERROR;
         if (!rc && active) ++b->replays;
         if (!rc) {
-            for (int i = 0; i < nm; ++i)
+            std::fill(rhs_busy.begin(), rhs_busy.end(), 0);
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (int i = 0; i < nm && !rc; ++i)
                 if (b->h_state[i].phase == PH_DONE) {
                     to_stats(b->h_state[i], &snap[i]);
                     const Geom& g = b->mem[i]->L[0].g;
@@ -1094,11 +1128,21 @@ void srv_loop(ples_srv* s) {
                     if (cudaMemcpyAsync(s->pin_fi[i], b->mem[i]->fi_c, sizeof(double) * box_count(g),
                                         cudaMemcpyDeviceToHost, b->st) != cudaSuccess)
                         rc = PLES_MG_CUDA_ERROR;
+                    s->handing[i] = s->inflight[i];
+                    s->inflight[i].reset();
                     b->h_state[i].phase = PH_IDLE;
                     dirty = true;
                     out_pending.push_back(i);
+                    if (!rc && s->prepared[i]) {  // the member's next request joins the next replay
+                        auto r = s->prepared[i];
+                        s->prepared[i].reset();
+                        s->inflight[i] = r;
+                        if ((rc = stage_in(b, i, nullptr, s->pin_rhs[i], false))) break;
+                        rhs_busy[i] = 1;
+                        admit(b, i, r->rel_tol, 0.0, r->max_cycles);
+                    }
                 }
-            if (!out_pending.empty() && cudaEventRecord(s->ev_out, b->st) != cudaSuccess) rc = PLES_MG_CUDA_ERROR;
+            if (!rc && !out_pending.empty() && cudaEventRecord(s->ev_out, b->st) != cudaSuccess) rc = PLES_MG_CUDA_ERROR;
         }
         if (rc) {  // a device error ends the server: fail everything in flight
             std::lock_guard<std::mutex> lk(s->mu);
@@ -1180,6 +1224,8 @@ int ples_srv_create(ples_mg_handle* const* members, int n, double hbm_budget_byt
     ples_srv* s = new ples_srv();
     s->eng = b;
     s->inflight.resize(n);
+    s->prepared.resize(n);
+    s->handing.resize(n);
     s->bytes = bytes;
     bool ok = cudaEventCreateWithFlags(&s->ev_out, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; i < n && ok; ++i) {
@@ -1236,7 +1282,8 @@ int ples_srv_wait(ples_srv* s, long long ticket, ples_mg_stats* stats) {
             }
         bool known = false;
         for (auto& r : s->pending) known = known || r->ticket == ticket;
-        for (auto& r : s->inflight) known = known || (r && r->ticket == ticket);
+        for (auto* v : {&s->inflight, &s->prepared, &s->handing})
+            for (auto& r : *v) known = known || (r && r->ticket == ticket);
         if (!known) return PLES_MG_BAD_ARG;
         s->cv_done.wait(lk);
     }

@@ -193,6 +193,38 @@ def test_server_warm_start_and_budget(cases):
         assert l2 <= 1e-8 and mx <= 1e-8
 
 
+def test_server_queued_requests_match_one_at_a_time(cases):
+    """Three requests queued at once for one member, beside a request for
+    another: the server stages the next right-hand side while the current
+    request solves and admits it as soon as that one finishes.  Each result
+    is the one the same requests give submitted one after another (each
+    warm-started from the solution before it), within 1e-12."""
+    x, y, z, rhs = cases[0]
+    other = cases[1]
+    rng = np.random.default_rng(11)
+    rhss = []
+    for _ in range(3):
+        r = rhs + 0.05 * np.abs(rhs).max() * rng.standard_normal(rhs.shape)
+        rhss.append(r - r.mean())
+    with mg.Multigrid(x, y, z) as m, mg.Multigrid(*other[:3]) as m2:
+        with mg.Server([m, m2]) as s:
+            seq = [s.wait(s.submit(0, r, rel_tol=REL_TOL)) for r in rhss]
+    with mg.Multigrid(x, y, z) as m, mg.Multigrid(*other[:3]) as m2:
+        with mg.Server([m, m2]) as s:
+            t_other = s.submit(1, other[3], rel_tol=REL_TOL)
+            tickets = [s.submit(0, r, rel_tol=REL_TOL) for r in rhss]
+            queued = [s.wait(t) for t in tickets]
+            _, st_other = s.wait(t_other)
+            rep = s.report()
+    assert st_other["status"] == mg.OK and rep["completed"] == 4
+    for (fa, sa), (fb, sb) in zip(seq, queued, strict=True):
+        assert sa["status"] == sb["status"] == mg.OK
+        assert sa["outer_iterations"] == sb["outer_iterations"]
+        assert np.abs(fb - fa).max() <= 1e-12 * np.abs(fa).max()
+    # the later requests started warm: no more outer iterations than the first
+    assert seq[2][1]["outer_iterations"] <= seq[0][1]["outer_iterations"]
+
+
 def test_autotune_then_batch(cases):
     """Tuned settings stay in their candidate sets, the tuned single-grid
     solve still converges to the oracle's solution, and a batch of tuned
