@@ -195,6 +195,24 @@ __device__ __forceinline__ void k_resid_outer2_df_blk(Geom g, Coef<float2> cs, c
     }
     for (int k = k0; k <= k1; ++k) {
         q = g.at(ic, jc, k);
+        // this warp's rows of plane k + 1 into L2, one 128-byte line per
+        // lane: lanes 0-17 the nine coefficient pairs, 18-19 b, 20-21 x one
+        // plane further (the differences run a plane ahead).  Measured on
+        // GB300 at 256x128x256: 394 -> 360 us per launch; two planes ahead
+        // gains no more
+        if (tx < 22 && k < k1) {
+            const long long q0 = g.at(B.x * 32 + 1, jc, k + 1) + (tx & 1) * 16;
+            const int u = tx >> 1;
+            if (u < 9) {
+                const float2* a = u == 0 ? cs.a1 : u == 1 ? cs.b12 : u == 2 ? cs.b13 : u == 3 ? cs.a2
+                                : u == 4 ? cs.b21 : u == 5 ? cs.b23 : u == 6 ? cs.a3 : u == 7 ? cs.b31 : cs.b32;
+                pf_l2(a, q0);
+            } else if (u == 9) {
+                pf_l2(b, q0);
+            } else {
+                pf_l2(x, q0 + sk);
+            }
+        }
         const int buf = k & 1;
         sDx[buf][ty][tx] = Dx0;
         sDz[buf][ty][tx] = Dz0;
