@@ -26,6 +26,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
+#include "gauss_jordan.cuh"
 #include "line_tma.cuh"
 #include "handle.h"
 #include "mg_device.cuh"
@@ -1027,8 +1028,9 @@ double mean_spacing(const double* x, const double* y, const double* z, int jx, i
     return n ? s / n : 1.0;
 }
 
-// Gauss-Jordan inversion with partial pivoting on the device (FP64), one
-// launch per pivot column.  K (m x m) is reduced to a row-permuted diagonal
+// Gauss-Jordan inversion with partial pivoting on the device, one launch
+// per pivot column: the form FP64 handles use (FP32 handles use the blocked
+// form of gauss_jordan.cuh, with the same pivots and result layout).  K (m x m) is reduced to a row-permuted diagonal
 // while the same row operations build E; the pivot rows stay where they are
 // and unscaled (row p_c keeps its pivot K(p_c, c), and the inverse's row c
 // is E's row p_c divided by it at the end).  So a step reads the pivot row,
@@ -1049,8 +1051,7 @@ double mean_spacing(const double* x, const double* y, const double* z, int jx, i
 // system singular.  Each column has kGjSlots keys, row r offering to slot
 // r mod kGjSlots (one address taking every row's atomic serialises the
 // step); the step that uses a column reduces its slots with one warp.
-// The matrix type R is FP64, or FP32 for a mixed handle, whose inverse is
-// stored in FP32 anyway (half the bytes per step; K and S then stay in L2).
+// The matrix type R is that of the stored inverse.
 constexpr int kGjSlots = 32;
 __device__ __forceinline__ unsigned gj_hi(double v) { return (unsigned)__double2hiint(v); }
 __device__ __forceinline__ unsigned gj_hi(float v) { return __float_as_uint(v); }
@@ -1240,7 +1241,13 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
     R *dK, *dI;
     unsigned long long* dKey;
     int *dUsed, *dPiv, *dBad;
+    R *dF = nullptr, *dW = nullptr;  // panel multipliers and w, B x m each (blocked FP32 form)
     int rc;
+    if constexpr (std::is_same<R, float>::value) {
+        if ((rc = talloc((void**)&dF, sizeof(R) * (size_t)m * GjPanel<R>::B)) ||
+            (rc = talloc((void**)&dW, sizeof(R) * (size_t)m * GjPanel<R>::B)))
+            return rc;
+    }
     if ((rc = talloc((void**)&dK64, 8 * (size_t)m * m)) ||
         (rc = talloc((void**)&dK, sizeof(R) * (size_t)m * m)) || (rc = talloc((void**)&dI, sizeof(R) * (size_t)m * m)) ||
         (rc = talloc((void**)&dKey, 8 * ((size_t)m + 1) * kGjSlots)) || (rc = talloc((void**)&dUsed, sizeof(int) * (size_t)m)) ||
@@ -1252,11 +1259,28 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         CK(cudaMemsetAsync(dI, 0, sizeof(R) * (size_t)m * m, h->st));
         CK(cudaMemsetAsync(dKey, 0, 8 * ((size_t)m + 1) * kGjSlots, h->st));
         CK(cudaMemsetAsync(dUsed, 0, sizeof(int) * (size_t)m, h->st));
+        CK(cudaMemsetAsync(dPiv, 0, sizeof(int) * (size_t)m, h->st));
         CK(cudaMemsetAsync(dBad, 0, sizeof(int), h->st));
-        k_gj_first<R><<<(m + 255) / 256, 256, 0, h->st>>>(dK, m, dKey);
-        for (int col = 0; col < m; ++col)
-            k_gj_step<R><<<m, 256, 0, h->st>>>(dK, dI, m, col, dKey, dUsed, dPiv, dBad);
-        h->launches += 1LL + m;
+        if constexpr (std::is_same<R, float>::value) {
+            // FP32 (mixed handles): blocked by panels (gauss_jordan.cuh);
+            // on GB300 at m = 2561, 17.9 against 41.8 ms for the column-by-
+            // column form below.  FP64 keeps that form: its rank-B updates
+            // run at the FP64 rate and the panels on one SM gain nothing.
+            constexpr int B = GjPanel<R>::B;
+            const size_t sm = gjb_panel_smem<R>(m);
+            CK(cudaFuncSetAttribute(k_gjb_panel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            for (int c0 = 0; c0 < m; c0 += B) {
+                const int nb = std::min(B, m - c0);
+                k_gjb_panel<R><<<1, kGjThreads, sm, h->st>>>(dK, dI, dF, dW, m, c0, nb, dUsed, dPiv, dBad);
+                k_gjb_update<R><<<dim3((m + 63) / 64, (m + 63) / 64), 256, 0, h->st>>>(dK, dI, dF, dW, m, c0, nb);
+                h->launches += 2;
+            }
+        } else {
+            k_gj_first<R><<<(m + 255) / 256, 256, 0, h->st>>>(dK, m, dKey);
+            for (int col = 0; col < m; ++col)
+                k_gj_step<R><<<m, 256, 0, h->st>>>(dK, dI, m, col, dKey, dUsed, dPiv, dBad);
+            h->launches += 1LL + m;
+        }
         CK(cudaGetLastError());
         int hbad = 0;
         CK(cudaMemcpyAsync(&hbad, dBad, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -1338,6 +1362,8 @@ void mask_coef(ples_mg_handle* h, int lev, Coef<T>& c) {
 // largest coarsest system solved by the dense inverse (unknowns, wall rows
 // included): coarsening stops at the first level at or below it
 constexpr int kDenseMax = 3072;
+static_assert(kDenseMax + 1 <= kGjThreads * kGjRows, "the blocked inverse's panel CTA owns at most 4 rows a thread");
+static_assert(gjb_panel_smem<float>(kDenseMax + 1) + 2048 <= 227 * 1024, "a panel of the blocked inverse fits shared memory");
 
 int lookup_norm_scratch(ples_mg_handle* h);
 
