@@ -88,8 +88,9 @@ __global__ void __launch_bounds__(kGjThreads, 1) k_gjb_panel(R* __restrict__ K, 
         }
         if (lane == 0) { s_best[buf][wid] = best; s_row[buf][wid] = br; }
         __syncthreads();
-        best = s_best[buf][lane];
-        br = s_row[buf][lane];
+        constexpr int nw = kGjThreads / 32;
+        best = lane < nw ? s_best[buf][lane] : R(0);
+        br = lane < nw ? s_row[buf][lane] : -1;
         for (int o = 16; o; o >>= 1) {
             const R v2 = __shfl_xor_sync(0xffffffffu, best, o);
             const int r2 = __shfl_xor_sync(0xffffffffu, br, o);
