@@ -350,7 +350,9 @@ void ples_mg_batch_destroy(ples_mg_batch *b);
  * request in flight and joins the next outer iteration of the members
  * already running, so the work of all admitted requests overlaps on the
  * device.  Each solve starts from its member's previous solution (warm
- * start; zero for the first).  Thread-safe. */
+ * start; zero for the first).  A member's requests are served in the order
+ * they were submitted; while one solves, the next one's right-hand side is
+ * staged, and it is admitted as soon as the first finishes.  Thread-safe. */
 typedef struct ples_srv ples_srv;
 int ples_srv_create(ples_mg_handle *const *members, int n, double hbm_budget_bytes, ples_srv **out);
 /* rhs (host, (1:jx,1:jy,1:jz)) is copied before the call returns; fi_out
