@@ -1054,7 +1054,6 @@ double mean_spacing(const double* x, const double* y, const double* z, int jx, i
 // The matrix type R is that of the stored inverse.
 constexpr int kGjSlots = 32;
 __device__ __forceinline__ unsigned gj_hi(double v) { return (unsigned)__double2hiint(v); }
-__device__ __forceinline__ unsigned gj_hi(float v) { return __float_as_uint(v); }
 template <typename R>
 __device__ __forceinline__ void gj_offer(unsigned long long* key, R v, int r, int m) {
     if (v > R(0))
@@ -1120,6 +1119,18 @@ __global__ void k_gj_extract(const R* __restrict__ K, const R* __restrict__ S,
     if (o < n) out[(size_t)c * n + o] = T(S[(size_t)r * m + j] / K[(size_t)r * m + c]);
 }
 
+// one nonzero of the coarsest-level matrix, and their scatter into the
+// zeroed device matrix in the elimination's type (each (row, column) once)
+struct GjEntry {
+    int row, col;
+    double v;
+};
+template <typename R>
+__global__ void k_gj_scatter(const GjEntry* __restrict__ e, long long ne, int m, R* __restrict__ K) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ne; q += (long long)gridDim.x * blockDim.x)
+        K[(size_t)e[q].row * m + e[q].col] = R(e[q].v);
+}
+
 // dense inverse of the bordered coarsest system [[M, v], [1^T, 0]] (M: the
 // level operator on interior cells and wall ghost rows, periodic in x/z;
 // v: its left null vector, +1 on interior rows and -1 on wall rows)
@@ -1145,7 +1156,13 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
     auto A3 = [&](long long q) { return (double)hc[6][q]; };
     auto B31 = [&](long long q) { return (double)hc[7][q]; };
     auto B32 = [&](long long q) { return (double)hc[8][q]; };
-    std::vector<double> K((size_t)m * m, 0.0);
+    // the matrix as its nonzero entries, each (row, column) accumulated in
+    // the order of the terms below (the values a dense assembly gives),
+    // scattered into the zeroed device matrix
+    std::vector<GjEntry> ents;
+    ents.reserve((size_t)m * 24);
+    std::vector<std::pair<int, double>> rowv;
+    std::vector<char> in_mean((size_t)n, 0);  // the border row's 1 (rows outside the null space: 0)
     auto unk = [&](int i, int j, int k) {
         i = (i - 1 + nx) % nx;
         k = (k - 1 + nz) % nz;
@@ -1155,14 +1172,23 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
         for (int i = 1; i <= nx; ++i)
             for (int j = 0; j < nj; ++j) {
                 const int row = unk(i, j, k);
-                double* R = &K[(size_t)row * m];
-                auto add = [&](int di, int dj, int dk, double v) { R[unk(i + di, j + dj, k + dk)] += v; };
+                rowv.clear();
+                double border = 0.0;  // the row's entry in the border column n
+                auto add = [&](int di, int dj, int dk, double v) {
+                    const int col = unk(i + di, j + dj, k + dk);
+                    for (auto& e : rowv)
+                        if (e.first == col) {
+                            e.second += v;
+                            return;
+                        }
+                    rowv.emplace_back(col, 0.0 + v);
+                };
                 if (j == 0) {  // bottom wall relation
                     const long long q = g.at(i, 0, k);
                     add(0, 0, 0, A2(q)); add(0, 1, 0, -A2(q));
                     add(1, 1, 0, -B21(q)); add(1, 0, 0, -B21(q)); add(-1, 1, 0, B21(q)); add(-1, 0, 0, B21(q));
                     add(0, 1, 1, -B23(q)); add(0, 0, 1, -B23(q)); add(0, 1, -1, B23(q)); add(0, 0, -1, B23(q));
-                    R[n] = -1.0;
+                    border = -1.0;
                 } else if (j == nj - 1 && h->fs) {  // top free-surface relation (PrS0 = 0), face ny
                     const long long q = g.at(i, ny, k);
                     add(0, 0, 0, A2(q)); add(0, -1, 0, A2(q));
@@ -1173,7 +1199,7 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
                     add(0, 0, 0, A2(q)); add(0, -1, 0, -A2(q));
                     add(1, 0, 0, B21(q)); add(1, -1, 0, B21(q)); add(-1, 0, 0, -B21(q)); add(-1, -1, 0, -B21(q));
                     add(0, 0, 1, B23(q)); add(0, -1, 1, B23(q)); add(0, 0, -1, -B23(q)); add(0, -1, -1, -B23(q));
-                    R[n] = -1.0;
+                    border = -1.0;
                 } else {  // interior: fdx - fsn + fsop - fsot + fav - find
                     const long long q = g.at(i, j, k), qw = q - 1, qs = q - g.sj, qb = q - g.sk;
                     // fdx
@@ -1200,30 +1226,26 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
                     add(0, 0, 0, -A3(qb)); add(0, 0, -1, A3(qb));
                     add(1, 0, 0, -B31(qb)); add(1, 0, -1, -B31(qb)); add(-1, 0, 0, B31(qb)); add(-1, 0, -1, B31(qb));
                     add(0, 1, 0, -B32(qb)); add(0, 1, -1, -B32(qb)); add(0, -1, 0, B32(qb)); add(0, -1, -1, B32(qb));
-                    R[n] = 1.0;
+                    border = 1.0;
+                }
+                // a row without any coefficient (a solid cell of a mask, a
+                // wall row next to one) becomes an identity row outside the
+                // null space and the mean
+                double sum = 0.0;
+                for (const auto& e : rowv) sum += std::fabs(e.second);
+                if (sum == 0.0) {
+                    ents.push_back({row, row, 1.0});
+                } else {
+                    in_mean[row] = 1;
+                    for (const auto& e : rowv) ents.push_back({row, e.first, e.second});
+                    if (border != 0.0 && !h->fs) ents.push_back({row, n, border});
                 }
             }
-    // rows without any coefficient (solid cells of a mask and the wall rows
-    // next to them) become identity rows outside the null space and the mean
-    for (int u = 0; u < n; ++u) {
-        double* R = &K[(size_t)u * m];
-        double sum = 0.0;
-        for (int v = 0; v < n; ++v) sum += std::fabs(R[v]);
-        if (sum == 0.0) {
-            R[u] = 1.0;
-            R[n] = 0.0;
-            K[(size_t)n * m + u] = 0.0;
-        } else {
-            K[(size_t)n * m + u] = 1.0;
-        }
-    }
-    if (h->fs) {  // a free surface removes the null space: the border unknown decouples
-        for (int u = 0; u < n; ++u) {
-            K[(size_t)u * m + n] = 0.0;
-            K[(size_t)n * m + u] = 0.0;
-        }
-        K[(size_t)n * m + n] = 1.0;
-    }
+    // the border row: 1 under every row in the null space; a free surface
+    // removes the null space and the border unknown decouples
+    for (int u = 0; u < n; ++u)
+        if (in_mean[u] && !h->fs) ents.push_back({n, u, 1.0});
+    if (h->fs) ents.push_back({n, n, 1.0});
     // Gauss-Jordan inverse with partial pivoting, on the device
     std::vector<void*> tmp;
     auto talloc = [&](void** p, size_t bytes) -> int {
@@ -1237,7 +1259,7 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
     };
     // the elimination runs in the type of the stored inverse
     using R = T;
-    double* dK64;
+    GjEntry* dEnt;
     R *dK, *dI;
     unsigned long long* dKey;
     int *dUsed, *dPiv, *dBad;
@@ -1248,14 +1270,15 @@ int build_coarse_inverse(ples_mg_handle* h, int lev, const Coef<T>& c) {
             (rc = talloc((void**)&dW, sizeof(R) * (size_t)m * GjPanel<R>::B)))
             return rc;
     }
-    if ((rc = talloc((void**)&dK64, 8 * (size_t)m * m)) ||
+    if ((rc = talloc((void**)&dEnt, sizeof(GjEntry) * std::max<size_t>(1, ents.size()))) ||
         (rc = talloc((void**)&dK, sizeof(R) * (size_t)m * m)) || (rc = talloc((void**)&dI, sizeof(R) * (size_t)m * m)) ||
         (rc = talloc((void**)&dKey, 8 * ((size_t)m + 1) * kGjSlots)) || (rc = talloc((void**)&dUsed, sizeof(int) * (size_t)m)) ||
         (rc = talloc((void**)&dPiv, sizeof(int) * (size_t)m)) || (rc = talloc((void**)&dBad, sizeof(int))))
         return rc;
     auto gj = [&]() -> int {
-        CK(cudaMemcpyAsync(dK64, K.data(), 8 * (size_t)m * m, cudaMemcpyHostToDevice, h->st));
-        k_convert<R, double><<<grid1((long long)m * m), 256, 0, h->st>>>((long long)m * m, dK64, dK);
+        CK(cudaMemcpyAsync(dEnt, ents.data(), sizeof(GjEntry) * ents.size(), cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemsetAsync(dK, 0, sizeof(R) * (size_t)m * m, h->st));
+        k_gj_scatter<R><<<grid1((long long)ents.size()), 256, 0, h->st>>>(dEnt, (long long)ents.size(), m, dK);
         CK(cudaMemsetAsync(dI, 0, sizeof(R) * (size_t)m * m, h->st));
         CK(cudaMemsetAsync(dKey, 0, 8 * ((size_t)m + 1) * kGjSlots, h->st));
         CK(cudaMemsetAsync(dUsed, 0, sizeof(int) * (size_t)m, h->st));
